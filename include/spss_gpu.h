@@ -1,0 +1,143 @@
+/*
+ * spss_gpu.h — C ABI of libspss_gpu.so, the GB300 (sm_103a) implementation of
+ * the pairwise-interaction hot path of raven91/spssLangevinIntegration.
+ *
+ * Plain pointers and sizes only.  Host arrays use the reference's AoS layout:
+ * double[n*s], s = 4 (x, y, phi, omega) for the first-order model and s = 6
+ * (x, y, v_x, v_y, phi, omega) for the second-order model, in the unit box.
+ * Every function returns SPSS_OK (0) or a negative SPSS_ERR_* code and never
+ * aborts.  A context owns one CUDA stream and device buffers; it is not
+ * thread-safe (like the reference classes, which keep function-local statics).
+ *
+ * Citations are to the reference source tree (file:line).
+ */
+#ifndef SPSS_GPU_H
+#define SPSS_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPSS_OK 0
+#define SPSS_ERR_INVALID_ARGUMENT (-1)
+#define SPSS_ERR_CUDA (-2)
+#define SPSS_ERR_OUT_OF_MEMORY (-3)
+#define SPSS_ERR_NOT_SUPPORTED (-4)
+#define SPSS_ERR_NONFINITE (-5)
+#define SPSS_ERR_SIZE (-6)
+
+/* Interaction routine (ParticleSystemFirstOrder.hpp:31-50, ParticleSystemSecondOrder.hpp:23-56). */
+#define SPSS_VARIANT_DISPATCH 0          /* EvaluateRhs: the reference's choice by interaction radius */
+#define SPSS_VARIANT_ALL_PAIRS 1         /* EvaluateInteractionsWithAllPairs */
+#define SPSS_VARIANT_LINKED_LIST 2       /* EvaluateInteractionsWithLinkedList */
+#define SPSS_VARIANT_VERLET 3            /* EvaluateInteractionsWithVerletNeighborList */
+#define SPSS_VARIANT_LINKED_LIST_VERLET 4/* EvaluateInteractionsWithLinkedListAndVerletNeighborList */
+#define SPSS_VARIANT_GLOBAL_FIELD 5      /* EvaluateInteractionsWithGlobalPolarOrderField (first order) */
+
+/* Arithmetic of a context. */
+#define SPSS_PRECISION_F64 0   /* the reference's FP64 arithmetic, operation for operation */
+#define SPSS_PRECISION_F32 1   /* GB300 path: 64-bit fixed-point positions, FP32 pair and stage math */
+
+/* Steppers (Steppers/RungeKutta4Stepper.hpp:15-42, StochasticEulerStepper.hpp:14-60,
+ * StochasticEulerStepperPtr.hpp:19-115, StochasticRungeKuttaStepperPtr.hpp:21-85). */
+#define SPSS_STEPPER_RK4 0
+#define SPSS_STEPPER_STOCHASTIC_EULER 1
+#define SPSS_STEPPER_STOCHASTIC_RUNGE_KUTTA 2
+
+typedef struct spss_params
+{
+  int model;       /* 1 first order, 2 second order */
+  int flavor;      /* first-order class: 0 ParticleSystemFirstOrder, 1 ParticleSystemFirstOrderPtr */
+  int n;           /* number of particles */
+  int variant;     /* SPSS_VARIANT_* used by the steppers */
+  int precision;   /* SPSS_PRECISION_* */
+  int nc_verlet;   /* cells per side of the Verlet build grid; 0 = int(1/rho) as the reference */
+  double v0, xi, xi_r, D_r, xi_phi, D_phi, sigma, rho, alpha;
+  double r_max;    /* Verlet radius; 0 = rho + 0.05 (ParticleSystemFirstOrderPtr.cpp:97-98) */
+  unsigned long long seed;   /* Philox key of the noise stream */
+  unsigned int replica;      /* replica index folded into the Philox counter */
+} spss_params;
+
+typedef struct spss_ctx spss_ctx;
+
+/* Construction: the ParticleSystem* constructors (ParticleSystemFirstOrder.cpp:12-66,
+ * ParticleSystemSecondOrder.cpp:12-70) together with the steppers' buffers. */
+int spss_create(const spss_params *params, spss_ctx **out);
+int spss_destroy(spss_ctx *ctx);
+const char *spss_error_string(int code);
+int spss_version(void);
+
+/* The system state the steppers advance, resident in device memory.
+ * Host AoS copies: SimulationEngine*::system_state_ handed to DoStep. */
+int spss_set_state(spss_ctx *ctx, const double *state, long len);
+int spss_get_state(spss_ctx *ctx, double *state, long len);
+
+/* ParticleSystem*::EvaluateRhs / EvaluateInteractionsWith* on host arrays
+ * (ParticleSystemFirstOrder.cpp:90-112, :162-649; ParticleSystemSecondOrder.cpp:85-113,
+ * :116-409).  k_next is read and written: components the reference leaves
+ * unwritten (isolated particles) keep the caller's values. */
+int spss_evaluate_rhs(spss_ctx *ctx, int variant, const double *state, const double *k_prev, double *k_next,
+                      double k_coef, double dt);
+/* is_higher_order_sde_integration_ and GetComplimentaryAlignmentForce
+ * (ParticleSystemFirstOrderPtr.hpp:72-73). */
+int spss_set_higher_order(spss_ctx *ctx, int on);
+int spss_get_complementary_force(spss_ctx *ctx, double *out, long len);
+/* SetNaturalFrequencies (ParticleSystemFirstOrder.cpp:85-88). */
+int spss_set_natural_frequencies(spss_ctx *ctx, const double *freqs, long len);
+
+/* CalculateMaxDisplacement (ParticleSystemFirstOrder.cpp:670-696) and the
+ * Verlet-list bookkeeping it drives. */
+int spss_calculate_max_displacement(spss_ctx *ctx, const double *total_displacement, long len);
+int spss_get_verlet_state(spss_ctx *ctx, double *accumulated_displacement, int *should_update_lists,
+                          int *uses_verlet_list);
+int spss_set_should_update_lists(spss_ctx *ctx, int flag);
+
+/* Lists of the most recent build, reference order (pre_linked_list_,
+ * linked_list_, verlet_list_; ParticleSystemFirstOrder.hpp:59-66).
+ * Offsets are CSR; *count receives the number of rows / entries. */
+int spss_get_pre_linked_list(spss_ctx *ctx, int *out, long len);
+int spss_get_cells(spss_ctx *ctx, int *offsets, long offsets_len, int *members, long members_len, int *ncell);
+int spss_get_verlet_lists(spss_ctx *ctx, int *offsets, long offsets_len, int *entries, long entries_len,
+                          long *total);
+
+/* Stepper::DoStep on the resident state (RungeKutta4Stepper.cpp:29-101,
+ * StochasticEulerStepper.hpp:33-51, StochasticEulerStepperPtr.hpp:40-73,
+ * StochasticRungeKuttaStepperPtr.hpp:40-76).  Gaussian noise comes from a
+ * counter-based Philox4x32-10 stream keyed by (seed, replica, step counter,
+ * particle), which advances by one per stochastic step. */
+int spss_step(spss_ctx *ctx, int stepper, double t, double dt);
+/* nsteps consecutive DoStep calls, issued as one CUDA graph launch where possible. */
+int spss_steps(spss_ctx *ctx, int stepper, double t0, double dt, int nsteps);
+/* Drop-in DoStep(particle_system, system_state, t, dt) on a host AoS array:
+ * copies it in, steps, copies it back (the host array is registered as
+ * pinned memory on first use). */
+int spss_step_host(spss_ctx *ctx, int stepper, double *state, long len, double t, double dt);
+int spss_get_step_counter(spss_ctx *ctx, unsigned long long *counter);
+int spss_set_step_counter(spss_ctx *ctx, unsigned long long counter);
+/* The Gaussian draws the stepper consumes at step counter `step`, in the
+ * reference's draw order per particle (what a replayed oracle must see). */
+int spss_noise(spss_ctx *ctx, int stepper, unsigned long long step, double *out, long len);
+
+/* PeriodicBoundaryConditions::ApplyPeriodicBoundaryConditions(system_state)
+ * (PeriodicBoundaryConditions.cpp:127-135) on the resident state. */
+int spss_apply_pbc(spss_ctx *ctx);
+
+/* Observer reductions (BinaryObserverFirstOrder.cpp:125-142,
+ * BinaryObserverSecondOrder.cpp:121-138), accumulated in FP64:
+ * out = {|<e^{i phi}>|, arg, |<v/|v|>|, arg}; first order repeats the phase pair. */
+int spss_order_parameters(spss_ctx *ctx, double *out4);
+/* AveragingObserver::operator() and the averaged state (AveragingObserver.cpp:29-69). */
+int spss_average_accumulate(spss_ctx *ctx);
+int spss_average_get(spss_ctx *ctx, double *mean_state, long len, int *count);
+
+int spss_synchronize(spss_ctx *ctx);
+/* Number of kernels this context launched since creation. */
+int spss_kernel_launches(spss_ctx *ctx, unsigned long long *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

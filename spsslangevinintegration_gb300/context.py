@@ -1,0 +1,174 @@
+"""Python handle on one spss_ctx (include/spss_gpu.h): thin, allocation-free
+wrappers that pass numpy arrays to the C ABI and raise on any error code."""
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+
+
+class Context:
+    """One particle system on the GPU: state, interaction routine, steppers."""
+
+    def __init__(self, model, n, rho, precision=N.PRECISION_F64, variant=N.VARIANT_DISPATCH, flavor=1, v0=0.0,
+                 xi=0.0, xi_r=0.0, D_r=0.0, xi_phi=0.0, D_phi=0.0, sigma=0.0, alpha=0.0, r_max=0.0, nc_verlet=0,
+                 seed=0, replica=0):
+        self.L = N.lib()
+        self.model, self.n = int(model), int(n)
+        self.s = 4 if self.model == 1 else 6
+        self.params = N.Params(self.model, flavor, self.n, variant, precision, nc_verlet, v0, xi, xi_r, D_r, xi_phi,
+                               D_phi, sigma, rho, alpha, r_max, seed, replica)
+        h = ctypes.c_void_p()
+        N.check(self.L.spss_create(ctypes.byref(self.params), ctypes.byref(h)), "spss_create")
+        self.h = h
+
+    # -- lifetime
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.spss_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def length(self):
+        return self.n * self.s
+
+    # -- state
+    def set_state(self, state):
+        state = N.f64(state)
+        N.check(self.L.spss_set_state(self.h, N.dptr(state), state.size), "spss_set_state")
+
+    def get_state(self):
+        out = np.empty(self.length)
+        N.check(self.L.spss_get_state(self.h, N.dptr(out), out.size), "spss_get_state")
+        return out
+
+    # -- right-hand side
+    def evaluate_rhs(self, variant, state, k_prev, k_next, k_coef, dt):
+        """EvaluateRhs semantics: returns k_next updated (input array untouched)."""
+        state, k_prev = N.f64(state), N.f64(k_prev)
+        out = np.array(k_next, dtype=np.float64, copy=True)
+        N.check(self.L.spss_evaluate_rhs(self.h, variant, N.dptr(state), N.dptr(k_prev), N.dptr(out), k_coef, dt),
+                "spss_evaluate_rhs")
+        return out
+
+    def set_higher_order(self, on):
+        N.check(self.L.spss_set_higher_order(self.h, int(bool(on))), "spss_set_higher_order")
+
+    def complementary_force(self):
+        out = np.empty(self.n)
+        N.check(self.L.spss_get_complementary_force(self.h, N.dptr(out), out.size), "spss_get_complementary_force")
+        return out
+
+    def set_natural_frequencies(self, f):
+        f = N.f64(f)
+        N.check(self.L.spss_set_natural_frequencies(self.h, N.dptr(f), f.size), "spss_set_natural_frequencies")
+
+    # -- Verlet bookkeeping
+    def calculate_max_displacement(self, td):
+        td = N.f64(td)
+        N.check(self.L.spss_calculate_max_displacement(self.h, N.dptr(td), td.size), "calculate_max_displacement")
+
+    def verlet_state(self):
+        acc = ctypes.c_double()
+        flag = ctypes.c_int()
+        uses = ctypes.c_int()
+        N.check(self.L.spss_get_verlet_state(self.h, ctypes.byref(acc), ctypes.byref(flag), ctypes.byref(uses)),
+                "spss_get_verlet_state")
+        return acc.value, flag.value, uses.value
+
+    def set_should_update_lists(self, flag):
+        N.check(self.L.spss_set_should_update_lists(self.h, int(flag)), "spss_set_should_update_lists")
+
+    # -- lists
+    def pre_linked_list(self):
+        out = np.empty(self.n, dtype=np.int32)
+        N.check(self.L.spss_get_pre_linked_list(self.h, N.iptr(out), out.size), "spss_get_pre_linked_list")
+        return out
+
+    def cells(self):
+        nc = ctypes.c_int()
+        N.check(self.L.spss_get_cells(self.h, None, 0, None, 0, ctypes.byref(nc)), "spss_get_cells")
+        off = np.empty(nc.value + 1, dtype=np.int32)
+        mem = np.empty(self.n, dtype=np.int32)
+        N.check(self.L.spss_get_cells(self.h, N.iptr(off), off.size, N.iptr(mem), mem.size, ctypes.byref(nc)),
+                "spss_get_cells")
+        return off, mem
+
+    def verlet_lists(self):
+        total = ctypes.c_long()
+        N.check(self.L.spss_get_verlet_lists(self.h, None, 0, None, 0, ctypes.byref(total)), "spss_get_verlet_lists")
+        off = np.empty(self.n + 1, dtype=np.int32)
+        ent = np.empty(max(total.value, 1), dtype=np.int32)
+        N.check(self.L.spss_get_verlet_lists(self.h, N.iptr(off), off.size, N.iptr(ent), ent.size,
+                                             ctypes.byref(total)), "spss_get_verlet_lists")
+        return off, ent[: total.value]
+
+    # -- steppers
+    def step(self, stepper, t, dt):
+        N.check(self.L.spss_step(self.h, stepper, t, dt), "spss_step")
+
+    def steps(self, stepper, t0, dt, nsteps):
+        N.check(self.L.spss_steps(self.h, stepper, t0, dt, int(nsteps)), "spss_steps")
+
+    def step_host(self, stepper, state, t, dt):
+        """Drop-in DoStep on a host float64 array (updated in place)."""
+        assert state.dtype == np.float64 and state.flags.c_contiguous
+        N.check(self.L.spss_step_host(self.h, stepper, N.dptr(state), state.size, t, dt), "spss_step_host")
+        return state
+
+    @property
+    def step_counter(self):
+        c = ctypes.c_ulonglong()
+        N.check(self.L.spss_get_step_counter(self.h, ctypes.byref(c)), "spss_get_step_counter")
+        return c.value
+
+    @step_counter.setter
+    def step_counter(self, v):
+        N.check(self.L.spss_set_step_counter(self.h, int(v)), "spss_set_step_counter")
+
+    def noise(self, stepper, step):
+        per = {N.RK4: 0, N.STOCHASTIC_EULER: 1 if self.model == 1 else 3,
+               N.STOCHASTIC_RUNGE_KUTTA: 2 if self.model == 1 else 6}[stepper]
+        out = np.empty(self.n * per)
+        if per:
+            N.check(self.L.spss_noise(self.h, stepper, int(step), N.dptr(out), out.size), "spss_noise")
+        return out
+
+    def apply_pbc(self):
+        N.check(self.L.spss_apply_pbc(self.h), "spss_apply_pbc")
+
+    # -- observers
+    def order_parameters(self):
+        out = np.empty(4)
+        N.check(self.L.spss_order_parameters(self.h, N.dptr(out)), "spss_order_parameters")
+        return out
+
+    def average_accumulate(self):
+        N.check(self.L.spss_average_accumulate(self.h), "spss_average_accumulate")
+
+    def average(self):
+        out = np.empty(self.length)
+        cnt = ctypes.c_int()
+        N.check(self.L.spss_average_get(self.h, N.dptr(out), out.size, ctypes.byref(cnt)), "spss_average_get")
+        return out, cnt.value
+
+    def synchronize(self):
+        N.check(self.L.spss_synchronize(self.h), "spss_synchronize")
+
+    @property
+    def kernel_launches(self):
+        c = ctypes.c_ulonglong()
+        N.check(self.L.spss_kernel_launches(self.h, ctypes.byref(c)), "spss_kernel_launches")
+        return c.value

@@ -1,0 +1,269 @@
+// Internal declarations shared by the translation units of libspss_gpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <vector>
+
+#include "../../include/spss_gpu.h"
+
+namespace spss
+{
+
+// ------------------------------------------------------------------ errors
+
+struct Status
+{
+  int code = SPSS_OK;
+};
+
+#define SPSS_CUDA_TRY(expr)                                  \
+  do                                                         \
+  {                                                          \
+    cudaError_t _e = (expr);                                 \
+    if (_e != cudaSuccess)                                   \
+    {                                                        \
+      ::spss::record_cuda_error(_e, #expr, __FILE__, __LINE__); \
+      return SPSS_ERR_CUDA;                                  \
+    }                                                        \
+  } while (0)
+
+#define SPSS_TRY(expr)          \
+  do                            \
+  {                             \
+    int _rc = (expr);           \
+    if (_rc != SPSS_OK) return _rc; \
+  } while (0)
+
+void record_cuda_error(cudaError_t e, const char *what, const char *file, int line);
+int check_launch(const char *what);
+
+// ------------------------------------------------------------------ Philox
+
+// Philox4x32-10 (Salmon, Moraes, Dror & Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC'11).  Counter = (particle, step lo, step hi,
+// replica << 8 | block), key = seed.
+struct Philox
+{
+  __host__ __device__ static inline uint4 generate(uint4 c, uint2 k)
+  {
+#pragma unroll
+    for (int r = 0; r < 10; ++r)
+    {
+      const uint64_t p0 = (uint64_t) 0xD2511F53u * c.x;
+      const uint64_t p1 = (uint64_t) 0xCD9E8D57u * c.z;
+      const uint32_t hi0 = (uint32_t) (p0 >> 32), lo0 = (uint32_t) p0;
+      const uint32_t hi1 = (uint32_t) (p1 >> 32), lo1 = (uint32_t) p1;
+      c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+      k.x += 0x9E3779B9u;
+      k.y += 0xBB67AE85u;
+    }
+    return c;
+  }
+};
+
+struct NoiseKey
+{
+  uint64_t seed;
+  uint32_t replica;
+  uint64_t step;
+};
+
+__device__ __forceinline__ uint4 philox_block(const NoiseKey &nk, uint32_t particle, uint32_t block)
+{
+  uint4 c = make_uint4(particle, (uint32_t) nk.step, (uint32_t) (nk.step >> 32), (nk.replica << 8) | block);
+  return Philox::generate(c, make_uint2((uint32_t) nk.seed, (uint32_t) (nk.seed >> 32)));
+}
+
+// Box-Muller on two 32-bit uniforms in (0, 1): FP64 variant for the
+// reference-arithmetic path, FP32 variant for the fast path.
+__device__ __forceinline__ void box_muller_f64(uint32_t a, uint32_t b, double &z0, double &z1)
+{
+  const double u1 = ((double) a + 0.5) * 2.3283064365386963e-10;
+  const double u2 = ((double) b + 0.5) * 2.3283064365386963e-10;
+  const double r = sqrt(-2.0 * log(u1));
+  double s, c;
+  sincospi(2.0 * u2, &s, &c);
+  z0 = r * c;
+  z1 = r * s;
+}
+
+__device__ __forceinline__ void box_muller_f32(uint32_t a, uint32_t b, float &z0, float &z1)
+{
+  const float u1 = ((float) (a >> 8) + 0.5f) * 5.9604644775390625e-8f;
+  const float u2 = ((float) (b >> 8) + 0.5f) * 5.9604644775390625e-8f;
+  const float r = sqrtf(-2.0f * logf(u1));
+  float s, c;
+  sincospif(2.0f * u2, &s, &c);
+  z0 = r * c;
+  z1 = r * s;
+}
+
+// Normal number d (0-based, reference draw order) of one particle at one step.
+__device__ __forceinline__ double normal_f64(const NoiseKey &nk, uint32_t particle, int d)
+{
+  const uint4 u = philox_block(nk, particle, (uint32_t) (d >> 2));
+  double z0, z1;
+  if ((d & 3) < 2) box_muller_f64(u.x, u.y, z0, z1);
+  else box_muller_f64(u.z, u.w, z0, z1);
+  return (d & 1) ? z1 : z0;
+}
+
+__device__ __forceinline__ void normals4_f32(const NoiseKey &nk, uint32_t particle, uint32_t block, float z[4])
+{
+  const uint4 u = philox_block(nk, particle, block);
+  box_muller_f32(u.x, u.y, z[0], z[1]);
+  box_muller_f32(u.z, u.w, z[2], z[3]);
+}
+
+__device__ __forceinline__ void normals4_f64(const NoiseKey &nk, uint32_t particle, uint32_t block, double z[4])
+{
+  const uint4 u = philox_block(nk, particle, block);
+  box_muller_f64(u.x, u.y, z[0], z[1]);
+  box_muller_f64(u.z, u.w, z[2], z[3]);
+}
+
+inline int normals_per_particle(int model, int stepper)
+{
+  if (stepper == SPSS_STEPPER_RK4) return 0;
+  if (stepper == SPSS_STEPPER_STOCHASTIC_EULER) return model == 1 ? 1 : 3;
+  return model == 1 ? 2 : 6;
+}
+
+// ------------------------------------------------------------------ device memory
+
+template<class T>
+struct DeviceArray
+{
+  T *ptr = nullptr;
+  size_t count = 0;
+  int reserve(size_t n)
+  {
+    if (n <= count && ptr) return SPSS_OK;
+    release();
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **) &ptr, n * sizeof(T));
+    if (e != cudaSuccess)
+    {
+      ptr = nullptr;
+      count = 0;
+      cudaGetLastError();
+      return SPSS_ERR_OUT_OF_MEMORY;
+    }
+    count = n;
+    return SPSS_OK;
+  }
+  void release()
+  {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    count = 0;
+  }
+  size_t bytes() const { return count * sizeof(T); }
+};
+
+// Exclusive prefix sum of `n` int32 counts into offsets[0..n] (offsets[n] =
+// total), three-phase with recursion on the block sums.
+struct Scanner
+{
+  std::vector<DeviceArray<int>> levels;
+  int run(const int *in, int *out, int n, cudaStream_t stream, unsigned long long &launches);
+  int run_level(const int *in, int *out, int n, size_t level, cudaStream_t stream, unsigned long long &launches);
+  void release()
+  {
+    for (auto &l : levels) l.release();
+    levels.clear();
+  }
+};
+
+// Stable cell binning: cell id per element -> CSR offsets and members that list
+// each cell's elements in ascending element order (the push_back order of the
+// reference's linked_list_, ParticleSystemFirstOrder.cpp:285-288).
+struct Binner
+{
+  DeviceArray<int> count, offsets, slot, members;
+  Scanner scanner;
+  int ncell = 0;
+  int run(const int *cell_of, int n, int ncell, cudaStream_t stream, unsigned long long &launches);
+  void release()
+  {
+    count.release();
+    offsets.release();
+    slot.release();
+    members.release();
+    scanner.release();
+  }
+};
+
+// ------------------------------------------------------------------ contexts
+
+struct F64Path;
+struct FastPath;
+
+}  // namespace spss
+
+struct spss_ctx
+{
+  spss_params p{};
+  int s = 4;
+  cudaStream_t stream = nullptr;
+  unsigned long long launches = 0;
+  unsigned long long step_counter = 0;
+  int higher_order = 0;
+  // Verlet bookkeeping (CalculateMaxDisplacement), kept on the host in FP64.
+  double accumulated_displacement = 0.0;
+  int should_update_lists = 1;
+  int uses_verlet_list = 0;
+  double r_min = 0.0, r_max = 0.0;
+  int nc = 1, nc_verlet = 1;
+  // host registration of the caller's array for spss_step_host
+  void *registered_host = nullptr;
+  size_t registered_bytes = 0;
+  spss::F64Path *f64 = nullptr;
+  spss::FastPath *fast = nullptr;
+  // AveragingObserver accumulator (FP64, AoS) and its count
+  spss::DeviceArray<double> average;
+  int average_count = 0;
+  // AoS staging buffers for host-array entry points
+  spss::DeviceArray<double> scratch_a, scratch_b, scratch_c;
+};
+
+namespace spss
+{
+// F64 (reference arithmetic) path, f64_path.cu
+int f64_create(spss_ctx *ctx);
+void f64_destroy(spss_ctx *ctx);
+int f64_set_state(spss_ctx *ctx, const double *d_aos);
+int f64_get_state(spss_ctx *ctx, double *d_aos);
+int f64_evaluate(spss_ctx *ctx, int variant, const double *d_state, const double *d_kprev, double *d_knext,
+                 double k_coef, double dt);
+int f64_step(spss_ctx *ctx, int stepper, double t, double dt);
+int f64_noise(spss_ctx *ctx, int stepper, unsigned long long step, double *d_out);
+int f64_max_displacement(spss_ctx *ctx, const double *d_td, double *max2_out);
+int f64_complementary_force(spss_ctx *ctx, double *d_out);
+int f64_set_natural_frequencies(spss_ctx *ctx, const double *d_freqs);
+int f64_lists(spss_ctx *ctx, int **pll, int **cell_off, int **cell_mem, int *ncell, int **vl_off, int **vl_ent,
+              long *vl_total);
+int f64_apply_pbc(spss_ctx *ctx);
+int f64_state_ptr(spss_ctx *ctx, const double **d_aos);
+
+// Fast (GB300) path, fast_path.cu
+int fast_create(spss_ctx *ctx);
+void fast_destroy(spss_ctx *ctx);
+int fast_set_state(spss_ctx *ctx, const double *d_aos);
+int fast_get_state(spss_ctx *ctx, double *d_aos);
+int fast_evaluate(spss_ctx *ctx, int variant, const double *d_state, const double *d_kprev, double *d_knext,
+                  double k_coef, double dt);
+int fast_step(spss_ctx *ctx, int stepper, double t, double dt);
+int fast_steps(spss_ctx *ctx, int stepper, double t0, double dt, int nsteps);
+int fast_noise(spss_ctx *ctx, int stepper, unsigned long long step, double *d_out);
+int fast_complementary_force(spss_ctx *ctx, double *d_out);
+int fast_apply_pbc(spss_ctx *ctx);
+
+// Shared helpers, spss_gpu.cu
+int order_parameters_aos(spss_ctx *ctx, const double *d_aos, double out[4]);
+int host_calculate_max_displacement(spss_ctx *ctx, double max2);
+int variant_for(const spss_ctx *ctx, int variant);
+}  // namespace spss
