@@ -1,0 +1,370 @@
+#!/usr/bin/env python
+"""Benchmark of the pairwise-interaction hot path on GB300.
+
+Workload (one step = one stochastic Runge-Kutta step of the whole system):
+second-order model, N = 4,194,304, density 2, interaction radius R = 1,
+Verlet list with skin 0.3 R rebuilt on the max-displacement trigger, strong
+order 1.5 stochastic Taylor stepper, dt = 0.005, inertia m = 1, v0 = 0.5,
+sigma = 1, D = 0.1; uniform random positions and phases (seeded synthetic
+field), mapped to the reference's unit box (L = sqrt(N / density)).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  `value`: particle-steps/s with the state resident in
+HBM (CUDA events on the library's stream, max over ranks, summed over ranks).
+`e2e`: the same through spss_step_host (host array in, host array out every
+step).  `roofline`: the pair-and-update kernel's algorithmic bytes over its
+CUDA-event duration.  `cpu_baseline` (rank 0): the oracle port of the
+reference algorithm on this host's cores.  `--impl reference` times the
+oracle port alone on the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT = 4194304
+DENSITY, RADIUS, SKIN, DT = 2.0, 1.0, 0.3, 0.005
+V0, MASS, SIGMA, NOISE = 0.5, 1.0, 1.0, 0.1
+SRK = 2
+L2_BYTES = 129 * 2 ** 20
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def workload(n):
+    """Physical configuration mapped to the reference's unit box."""
+    L = np.sqrt(n / DENSITY)
+    rho = RADIUS / L
+    r_max = (1.0 + SKIN) * rho
+    return dict(model=2, n=n, rho=rho, v0=V0 / L, xi_r=1.0 / MASS, xi_phi=1.0 / MASS, D_r=0.0,
+                D_phi=NOISE / MASS ** 2, sigma=SIGMA / MASS, alpha=0.0, r_max=r_max, nc_verlet=int(1.0 / r_max)), L
+
+
+def initial_state(n, L, seed):
+    rng = np.random.default_rng(seed)
+    x = np.empty((n, 6))
+    x[:, 0] = rng.random(n)
+    x[:, 1] = rng.random(n)
+    phi = rng.uniform(-np.pi, np.pi, n)
+    x[:, 2] = np.cos(phi) / L
+    x[:, 3] = np.sin(phi) / L
+    x[:, 4] = phi
+    x[:, 5] = 0.0
+    return x.reshape(-1)
+
+
+def mean_list_length(p):
+    """Expected Verlet candidates per particle: pi r_max^2 n (unit box)."""
+    return np.pi * p["r_max"] ** 2 * p["n"]
+
+
+def algorithmic_bytes_per_particle(p):
+    """Pair-and-update kernel, per particle-step: the 32-byte state read and
+    written once (positions 2 x 8 B fixed point, v_x, v_y, phase, omega 4 B
+    each) plus the Verlet list (4 B count + 4 B per entry)."""
+    return 32 * 2 + 4 + 4 * mean_list_length(p)
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [c.strip() for c in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def hbm_peak():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def traffic_per_launch():
+    """DRAM bytes per launch of the pair-and-update kernel from the committed
+    ncu summary (profiles/), scaled to the full system; None before a capture."""
+    path = os.path.join(ROOT, "profiles", "fast_step_srk2_verlet.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["dram_bytes_per_particle"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def cpu_baseline(n, budget_s=20.0, bench_lib=True):
+    """The oracle port (FP64, OpenMP over particles as the reference's MPI
+    decomposition) on this host's cores, on the same workload, for a bounded
+    number of steps."""
+    from oracle import binding as ob
+
+    cores = os.cpu_count() or 1
+    ob.set_threads(cores, bench=bench_lib)
+    p, L = workload(n)
+    sysm = ob.System(2, n, p["rho"], v0=p["v0"], xi_r=p["xi_r"], D_r=p["D_r"], xi_phi=p["xi_phi"],
+                     D_phi=p["D_phi"], sigma=p["sigma"], alpha=p["alpha"], r_max=p["r_max"],
+                     nc_verlet=p["nc_verlet"], bench=bench_lib)
+    x = initial_state(n, L, 0)
+    # warm-up step builds the Verlet list
+    sysm.step(ob.SRK, 4, x, DT, DT, ob.philox_normals(0, 0, 0, 6 * n, bench=bench_lib))
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        normals = ob.philox_normals(0, steps + 1, 0, 6 * n, bench=bench_lib)
+        sysm.step(ob.SRK, 4, x, DT * (steps + 2), DT, normals)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or steps >= 50:
+            break
+    sysm.close()
+    return {"value": n * steps / el, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+            "sample": "N=%d second-order SRK, linked-list+Verlet skin 0.3R, %d timed steps after 1 warm-up "
+                      "step (%.1f s), FP64 oracle port, OpenMP %d threads" % (n, steps, el, cores)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    n = args.n
+    res = None
+    per_step = []
+    # W untimed samples then K timed ones, each sample one oracle-port step
+    from oracle import binding as ob
+
+    cores = os.cpu_count() or 1
+    ob.set_threads(cores, bench=True)
+    p, L = workload(n)
+    sysm = ob.System(2, n, p["rho"], v0=p["v0"], xi_r=p["xi_r"], D_r=p["D_r"], xi_phi=p["xi_phi"],
+                     D_phi=p["D_phi"], sigma=p["sigma"], alpha=p["alpha"], r_max=p["r_max"],
+                     nc_verlet=p["nc_verlet"], bench=True)
+    x = initial_state(n, L, 0)
+    budget = 120.0
+    t_start = time.perf_counter()
+    for k in range(args.warmup + args.steps):
+        normals = ob.philox_normals(0, k, 0, 6 * n, bench=True)
+        t0 = time.perf_counter()
+        sysm.step(ob.SRK, 4, x, DT * (k + 1), DT, normals)
+        dt_s = time.perf_counter() - t0
+        if k >= args.warmup:
+            per_step.append(dt_s)
+        if time.perf_counter() - t_start > budget and len(per_step) >= 1:
+            break
+    sysm.close()
+    total = sum(per_step)
+    value = n * len(per_step) / total
+    line = {
+        "impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+        "n_gpus": world, "steps": len(per_step), "warmup": args.warmup, "ms_per_step": 1e3 * total / len(per_step),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "second-order model, N=%d, density 2, R=1, Verlet skin 0.3R, StochasticRungeKutta, "
+                               "dt=0.005, m=1, v0=0.5, sigma=1, D=0.1" % n, "n": n},
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                         "sample": "%d timed SRK steps of the full N=%d system (FP64 oracle port, OpenMP %d threads)"
+                                   % (len(per_step), n, cores)},
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    from spsslangevinintegration_gb300 import PRECISION_F32, Context, LINKED_LIST_VERLET
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+    n = args.n
+    p, L = workload(n)
+    x0 = initial_state(n, L, seed=rank)
+    ctx = Context(2, n, p["rho"], precision=PRECISION_F32, variant=LINKED_LIST_VERLET, v0=p["v0"], xi_r=p["xi_r"],
+                  D_r=p["D_r"], xi_phi=p["xi_phi"], D_phi=p["D_phi"], sigma=p["sigma"], alpha=p["alpha"],
+                  r_max=p["r_max"], nc_verlet=p["nc_verlet"], seed=12345, replica=rank)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_state(x0)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # warm-up (includes graph capture and the first list build)
+    t = 0.0
+    ctx.steps(SRK, t, DT, args.warmup)
+    t += DT * args.warmup
+    barrier()
+    launches0 = ctx.kernel_launches
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clocks:
+        barrier()
+        e0.record(stream)
+        ctx.steps(SRK, t, DT, args.steps)
+        e1.record(stream)
+        barrier()
+    t += DT * args.steps
+    ms = e0.elapsed_time(e1)
+    launches = ctx.kernel_launches - launches0
+    if dist is not None:
+        tm = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
+        ms = float(tm.item())
+    value = world * n * args.steps / (ms * 1e-3)
+
+    # roofline: the pair-and-update kernel alone, CUDA events on the same stream
+    ctx.set_timing(True)
+    ctx.steps(SRK, t, DT, args.steps)
+    t += DT * args.steps
+    kernel_ms, kernel_count = ctx.timing()
+    ctx.set_timing(False)
+    avg_kernel_s = kernel_ms / max(kernel_count, 1) * 1e-3
+    peak, peak_kind = hbm_peak()
+    bytes_per_launch = n * algorithmic_bytes_per_particle(p)
+    achieved = bytes_per_launch / avg_kernel_s / 1e9
+    traffic = traffic_per_launch()
+
+    # end to end through the host-array entry point (the drop-in DoStep path)
+    host = ctx.get_state()
+    e2e_steps = max(1, min(args.steps, 10))
+    ctx.step_host(SRK, host, t, DT)  # registers the host array (pinned) once
+    t += DT
+    barrier()
+    w0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        ctx.step_host(SRK, host, t, DT)
+        t += DT
+    barrier()
+    e2e_s = time.perf_counter() - w0
+    if dist is not None:
+        tm = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
+        e2e_s = float(tm.item())
+    e2e_value = world * n * e2e_steps / e2e_s
+    acc, flag, uses = ctx.verlet_state()
+    ctx.close()
+
+    if rank != 0:
+        return 0
+    line = {
+        "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak" if world > 1 else "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "second-order model, N=%d, density 2, R=1, Verlet skin 0.3R (rebuilt on the "
+                               "max-displacement trigger), StochasticRungeKutta (strong order 1.5), dt=0.005, m=1, "
+                               "v0=0.5, sigma=1, D=0.1; one independent replica per GPU" % n,
+                   "n": n, "l2": "inputs larger than L2 (state %.0f MB + lists %.0f MB)" % (
+                       n * 56 / 1e6, n * 4 * (mean_list_length(p) + 1) / 1e6),
+                   "parallelism": "replicas x%d" % world},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "kernel": "fast_step_kernel<2,2,2> (pair sums + SRK update)",
+                     "kernel_ms": avg_kernel_s * 1e3,
+                     "algorithmic_bytes_per_particle": algorithmic_bytes_per_particle(p),
+                     "traffic": None if traffic is None else traffic * n},
+        "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": n * 6 * 8,
+                "d2h_bytes_per_step": n * 6 * 8, "steps": e2e_steps,
+                "path": "spss_step_host: host AoS float64 in, one SRK step, host AoS out"},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "verlet": {"accumulated_displacement": acc, "rebuild_pending": flag},
+    }
+    if not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_baseline(n, budget_s=args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    rc = run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -136,6 +136,17 @@ int spss_synchronize(spss_ctx *ctx);
 /* Number of kernels this context launched since creation. */
 int spss_kernel_launches(spss_ctx *ctx, unsigned long long *count);
 
+/* Issue all work of the context on the caller's CUDA stream (a cudaStream_t;
+ * NULL returns to the context's own stream).  No reference counterpart: the
+ * reference is CPU code. */
+int spss_set_stream(spss_ctx *ctx, void *cuda_stream);
+/* While timing is on, steps run one by one with CUDA events recorded on the
+ * context's stream around the pair-and-update kernel; spss_get_timing returns
+ * the summed kernel milliseconds and the number of timed launches.  No
+ * reference counterpart. */
+int spss_set_timing(spss_ctx *ctx, int on);
+int spss_get_timing(spss_ctx *ctx, double *kernel_ms, unsigned long long *timed_launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -86,6 +86,9 @@ SIGNATURES = {
     "spss_average_get": (_i, [_vp, _dp, _l, _ip]),
     "spss_synchronize": (_i, [_vp]),
     "spss_kernel_launches": (_i, [_vp, P(_ull)]),
+    "spss_set_stream": (_i, [_vp, _vp]),
+    "spss_set_timing": (_i, [_vp, _i]),
+    "spss_get_timing": (_i, [_vp, _dp, P(_ull)]),
 }
 
 

@@ -167,6 +167,19 @@ class Context:
     def synchronize(self):
         N.check(self.L.spss_synchronize(self.h), "spss_synchronize")
 
+    def set_stream(self, stream_handle):
+        """Issue work on a caller's cudaStream_t (an int handle; 0/None: own stream)."""
+        N.check(self.L.spss_set_stream(self.h, ctypes.c_void_p(stream_handle or None)), "spss_set_stream")
+
+    def set_timing(self, on):
+        N.check(self.L.spss_set_timing(self.h, int(bool(on))), "spss_set_timing")
+
+    def timing(self):
+        ms = ctypes.c_double()
+        cnt = ctypes.c_ulonglong()
+        N.check(self.L.spss_get_timing(self.h, ctypes.byref(ms), ctypes.byref(cnt)), "spss_get_timing")
+        return ms.value, cnt.value
+
     @property
     def kernel_launches(self):
         c = ctypes.c_ulonglong()

@@ -1,16 +1,1032 @@
-// GB300 fast path (placeholder until the fixed-point/FP32 kernels land).
+// GB300 fast path: fixed-point positions, FP32 pair and stage arithmetic,
+// fused pair sums + stochastic stepper update + Philox noise.
+//
+// Representation (slot order; slots are re-sorted by cell at every rebuild):
+//   rec[2][n]  uint4 {x_hi, y_hi, phase, omega bits}  double-buffered: a step
+//              reads rec[parity] (neighbours see the previous state) and
+//              writes rec[parity ^ 1]
+//   lo[2][n]   uint2 {x_lo, y_lo}, double-buffered with rec
+//   vel[n]     float2 {v_x, v_y} (second-order model)
+//   pid[n]     original particle index (noise counter, output order)
+//   img[n]     int2 box crossings since upload; turns[n] 2*pi turns of phase
+// x = img + (x_hi * 2^32 + x_lo) * 2^-64 (unit box), phase = 2*pi*(turns + phase * 2^-32).
+//
+// FP64 appears only where the result must not depend on FP32 rounding: the
+// exact cutoff decision inside a guard band around r = rho (a few pairs per
+// step), the accumulated Verlet displacement and the upload/download
+// conversions.  GB300 runs FP64 at about 1/70 of its FP32 rate.
+//
+// Reference semantics mirrored: ParticleSystemFirstOrder.cpp / ParticleSystemFirstOrderPtr.cpp
+// (pair sums, isolated particles keep zero torque derivative in SE/SRK),
+// ParticleSystemSecondOrder.cpp, StochasticEulerStepper.hpp:33-51,
+// StochasticEulerStepperPtr.hpp:40-73, StochasticRungeKuttaStepperPtr.hpp:40-76,
+// CalculateMaxDisplacement ParticleSystemFirstOrder.cpp:670-696.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <utility>
+
 #include "spss_internal.cuh"
 
 namespace spss
 {
-int fast_create(spss_ctx *) { return SPSS_ERR_NOT_SUPPORTED; }
-void fast_destroy(spss_ctx *) {}
-int fast_set_state(spss_ctx *, const double *) { return SPSS_ERR_NOT_SUPPORTED; }
-int fast_get_state(spss_ctx *, double *) { return SPSS_ERR_NOT_SUPPORTED; }
-int fast_evaluate(spss_ctx *, int, const double *, const double *, double *, double, double) { return SPSS_ERR_NOT_SUPPORTED; }
-int fast_step(spss_ctx *, int, double, double) { return SPSS_ERR_NOT_SUPPORTED; }
-int fast_steps(spss_ctx *, int, double, double, int) { return SPSS_ERR_NOT_SUPPORTED; }
-int fast_noise(spss_ctx *, int, unsigned long long, double *) { return SPSS_ERR_NOT_SUPPORTED; }
-int fast_complementary_force(spss_ctx *, double *) { return SPSS_ERR_NOT_SUPPORTED; }
-int fast_apply_pbc(spss_ctx *) { return SPSS_ERR_NOT_SUPPORTED; }
+
+constexpr int kTB = 256;
+
+struct FastControl
+{
+  unsigned long long step;  // Philox step counter of the next stochastic step
+  double acc;               // accumulated displacement (FP64)
+  int parity;               // current rec/lo buffer
+  int rebuild;              // lists (and slot order) rebuilt before the next evaluation
+  unsigned int max2_bits;   // max |dr|^2 of the step, FP32 bits (non-negative floats order as ints)
+  int overflow;             // largest Verlet count seen beyond capacity (0: none)
+  int rebuilds;             // number of rebuilds performed
+  int error;                // bit 0: displacement too large for the fixed-point increment
+  int uses_verlet;
+  int pad;
+};
+
+enum Kind
+{
+  KIND_ALL_PAIRS = 0,
+  KIND_CELLS = 1,
+  KIND_VERLET = 2
+};
+
+struct FastParams
+{
+  int n, nc, cap, model;
+  int kind, always_rebuild, pad0, pad1;
+  float v0, xi, xi_r, xi_phi, sigma, ca, sa;
+  float rho2_f, band_f, rmax2_f;
+  double rho2_d, half_skin;
+  float dt, sqdt, half_dt2, half_dt15, inv_sqrt3, b_r, b_phi;
+  uint64_t seed;
+  uint32_t replica;
+};
+
+struct FastBuffers
+{
+  uint4 *rec0, *rec1;
+  uint2 *lo0, *lo1;
+  float2 *vel, *vel_tmp;
+  unsigned *pid, *pid_tmp;
+  int2 *img, *img_tmp;
+  int *turns, *turns_tmp;
+  int *cell_of, *cell_sorted;
+  const int *cell_off;
+  const int *order;
+  int *vl, *vl_cnt;
+  float *caf;
+  FastControl *ctrl;
+};
+
+struct GraphEntry
+{
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  int per_step = 0;     // kernels of the unconditional part
+  int per_rebuild = 0;  // kernels of the conditional rebuild
+};
+
+struct FastPath
+{
+  DeviceArray<uint4> rec[2];
+  DeviceArray<uint2> lo[2];
+  DeviceArray<float2> vel, vel_tmp;
+  DeviceArray<unsigned> pid, pid_tmp;
+  DeviceArray<int2> img, img_tmp;
+  DeviceArray<int> turns, turns_tmp, cell_of, cell_sorted, vl, vl_cnt;
+  DeviceArray<float> caf;
+  Binner binner;
+  FastControl *ctrl = nullptr;    // device
+  FastControl *h_ctrl = nullptr;  // pinned mirror
+  int kind = KIND_CELLS;
+  int nc_build = 1;
+  int cap = 0;
+  bool have_state = false;
+  bool perm_valid = false;
+  std::map<std::pair<int, double>, GraphEntry> graphs;
+};
+
+// ---------------------------------------------------------------- helpers
+
+__device__ __forceinline__ uint64_t join64(uint32_t hi, uint32_t lo)
+{
+  return ((uint64_t) hi << 32) | lo;
+}
+
+// round-toward-zero f * 2^64 as a signed integer, exact for the 24-bit
+// mantissa; |f| < 0.5 (one step never moves a particle half a box).
+__device__ __forceinline__ long long fix64_of(float f, int &err)
+{
+  const uint32_t b = __float_as_uint(f);
+  const int e = (int) ((b >> 23) & 0xffu);
+  if (e == 0) return 0;
+  if (e >= 126)
+  {
+    err = 1;
+    return 0;
+  }
+  const long long m = (long long) ((b & 0x7fffffu) | 0x800000u);
+  const int sh = e - 86;
+  long long v = sh >= 0 ? (m << sh) : (sh > -24 ? (m >> (-sh)) : 0);
+  return (b >> 31) ? -v : v;
+}
+
+// X += dX on the periodic unit box; the image counter follows the carry.
+__device__ __forceinline__ uint64_t advance(uint64_t X, long long dX, int &img)
+{
+  const uint64_t Y = X + (uint64_t) dX;
+  if (dX > 0 && Y < X) ++img;
+  if (dX < 0 && Y > X) --img;
+  return Y;
+}
+
+__device__ __forceinline__ uint32_t advance_phase(uint32_t P, float dphi, int &turns, int &err)
+{
+  // 2^32 / (2 pi)
+  const float q = dphi * 683565275.5764316f;
+  if (!(fabsf(q) < 2.1e9f))
+  {
+    err = 1;
+    return P;
+  }
+  const int d = __float2int_rn(q);
+  const uint32_t R = P + (uint32_t) d;
+  if (d > 0 && R < P) ++turns;
+  if (d < 0 && R > P) --turns;
+  return R;
+}
+
+__device__ __forceinline__ void phase_sincos(uint32_t P, float &s, float &c)
+{
+  sincospif((float) (int) P * 4.656612873077393e-10f, &s, &c);  // P * 2^-31 in [-1, 1)
+}
+
+__device__ __forceinline__ int cell_of_fix(uint64_t X, uint64_t Y, int nc)
+{
+  const int cx = (int) __umul64hi(X, (uint64_t) nc);
+  const int cy = (int) __umul64hi(Y, (uint64_t) nc);
+  return cy * nc + cx;
+}
+
+__device__ __forceinline__ int wrap_cell(int c, int nc)
+{
+  return c < 0 ? nc - 1 : (c >= nc ? 0 : c);
+}
+
+struct Acc
+{
+  float ss, sc, ws, wc;
+  int card;
+};
+
+// One candidate pair: FP32 distance from the 32-bit high words (exact minimum
+// image by integer subtraction); inside the guard band the decision is
+// recomputed in FP64 from the full 64-bit positions, so it equals the FP64
+// decision for these positions.
+__device__ __forceinline__ void candidate(const FastParams &P, const uint4 &ri, uint64_t Xi, uint64_t Yi,
+                                          const uint4 &rj, const uint2 *lo, int j, Acc &a)
+{
+  const float dx = (float) (int) (rj.x - ri.x) * 2.3283064365386963e-10f;
+  const float dy = (float) (int) (rj.y - ri.y) * 2.3283064365386963e-10f;
+  const float d2 = fmaf(dx, dx, dy * dy);
+  bool in = d2 <= P.rho2_f;
+  if (fabsf(d2 - P.rho2_f) <= P.band_f)
+  {
+    const uint2 l = lo[j];
+    const double ex = (double) (long long) (join64(rj.x, l.x) - Xi) * 5.421010862427522e-20;
+    const double ey = (double) (long long) (join64(rj.y, l.y) - Yi) * 5.421010862427522e-20;
+    in = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)) <= P.rho2_d;
+  }
+  if (in)
+  {
+    float s, c;
+    phase_sincos(rj.z - ri.z, s, c);  // sin, cos of phi_j - phi_i
+    const float wj = __uint_as_float(rj.w);
+    a.ss += s;
+    a.sc += c;
+    a.ws += wj * s;
+    a.wc += wj * c;
+    a.card += 1;
+  }
+}
+
+// ---------------------------------------------------------------- conversions
+
+// Upload from reference AoS (original order).  With a valid slot order the
+// particle in slot q is pid[q]; otherwise slots are reset to the identity.
+__global__ void fast_upload_kernel(const double *__restrict__ x, int n, int s, int model, int perm_valid,
+                                   FastBuffers B)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int par = B.ctrl->parity;
+  const unsigned p = perm_valid ? B.pid[q] : (unsigned) q;
+  if (!perm_valid) B.pid[q] = p;
+  const double *st = x + (long) s * p;
+  int2 im;
+  uint64_t X, Y;
+  {
+    const double fx = floor(st[0]), fy = floor(st[1]);
+    im = make_int2((int) fx, (int) fy);
+    const double rx = st[0] - fx, ry = st[1] - fy;
+    X = (rx * 18446744073709551616.0 >= 18446744073709551615.0) ? ~0ull : __double2ull_rz(rx * 18446744073709551616.0);
+    Y = (ry * 18446744073709551616.0 >= 18446744073709551615.0) ? ~0ull : __double2ull_rz(ry * 18446744073709551616.0);
+  }
+  const int ip = model == 1 ? 2 : 4;
+  const double t = st[ip] * 0.15915494309189535;  // phi / (2 pi)
+  const double ft = floor(t);
+  const double fr = (t - ft) * 4294967296.0;
+  const uint32_t ph = fr >= 4294967295.0 ? 0xffffffffu : (uint32_t) fr;
+  const float w = (float) st[ip + 1];
+  uint4 r = make_uint4((uint32_t) (X >> 32), (uint32_t) (Y >> 32), ph, __float_as_uint(w));
+  uint4 *rec = par ? B.rec1 : B.rec0;
+  uint2 *lo = par ? B.lo1 : B.lo0;
+  rec[q] = r;
+  lo[q] = make_uint2((uint32_t) X, (uint32_t) Y);
+  B.img[q] = im;
+  B.turns[q] = (int) ft;
+  if (model == 2) B.vel[q] = make_float2((float) st[2], (float) st[3]);
+}
+
+__global__ void fast_download_kernel(double *__restrict__ x, int n, int s, int model, FastBuffers B)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  const int par = B.ctrl->parity;
+  const uint4 r = (par ? B.rec1 : B.rec0)[q];
+  const uint2 l = (par ? B.lo1 : B.lo0)[q];
+  const unsigned p = B.pid[q];
+  const int2 im = B.img[q];
+  double *st = x + (long) s * p;
+  st[0] = (double) im.x + (double) join64(r.x, l.x) * 5.421010862427522e-20;
+  st[1] = (double) im.y + (double) join64(r.y, l.y) * 5.421010862427522e-20;
+  const int ip = model == 1 ? 2 : 4;
+  st[ip] = 6.283185307179586 * ((double) B.turns[q] + (double) r.z * 2.3283064365386963e-10);
+  st[ip + 1] = (double) __uint_as_float(r.w);
+  if (model == 2)
+  {
+    const float2 v = B.vel[q];
+    st[2] = v.x;
+    st[3] = v.y;
+  }
+}
+
+// ---------------------------------------------------------------- rebuild
+
+__global__ void fast_cells_kernel(FastParams P, FastBuffers B)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= P.n) return;
+  const int par = B.ctrl->parity;
+  const uint4 r = (par ? B.rec1 : B.rec0)[q];
+  const uint2 l = (par ? B.lo1 : B.lo0)[q];
+  B.cell_of[q] = cell_of_fix(join64(r.x, l.x), join64(r.y, l.y), P.nc);
+}
+
+// New slot q takes the particle of old slot order[q] (cells contiguous,
+// ascending old slot inside a cell).  Writes the other rec/lo buffer.
+__global__ void fast_permute_kernel(FastParams P, FastBuffers B)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= P.n) return;
+  const int par = B.ctrl->parity;
+  const int src = B.order[q];
+  const uint4 *rin = par ? B.rec1 : B.rec0;
+  uint4 *rout = par ? B.rec0 : B.rec1;
+  const uint2 *lin = par ? B.lo1 : B.lo0;
+  uint2 *lout = par ? B.lo0 : B.lo1;
+  rout[q] = rin[src];
+  lout[q] = lin[src];
+  B.pid_tmp[q] = B.pid[src];
+  B.img_tmp[q] = B.img[src];
+  B.turns_tmp[q] = B.turns[src];
+  if (P.model == 2) B.vel_tmp[q] = B.vel[src];
+  B.cell_sorted[q] = B.cell_of[src];
+}
+
+__global__ void fast_copyback_kernel(FastParams P, FastBuffers B)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= P.n) return;
+  B.pid[q] = B.pid_tmp[q];
+  B.img[q] = B.img_tmp[q];
+  B.turns[q] = B.turns_tmp[q];
+  if (P.model == 2) B.vel[q] = B.vel_tmp[q];
+}
+
+// The permuted state lives in the other buffer; lists are now current.
+__global__ void fast_after_rebuild_kernel(FastControl *ctrl, int permuted)
+{
+  if (permuted) ctrl->parity ^= 1;
+  ctrl->rebuild = 0;
+  ctrl->rebuilds += 1;
+}
+
+// Verlet lists from the 3x3 stencil of the rebuild grid (ParticleSystemFirstOrder.cpp:536-589):
+// pairs with r <= r_max (conservatively widened by the guard band; an entry
+// beyond r_max can never come within rho before the next rebuild).  Entry m of
+// slot q at vl[m * n + q]; a count of -1 marks a list longer than the capacity.
+__global__ void fast_verlet_build_kernel(FastParams P, FastBuffers B)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= P.n) return;
+  const int par = B.ctrl->parity;
+  const uint4 *rec = par ? B.rec1 : B.rec0;
+  const uint4 ri = rec[q];
+  const int c = B.cell_sorted[q];
+  const int cx = c % P.nc, cy = c / P.nc;
+  int cnt = 0;
+  for (int sy = -1; sy <= 1; ++sy)
+  {
+    const int jy = wrap_cell(cy + sy, P.nc);
+    for (int sx = -1; sx <= 1; ++sx)
+    {
+      const int jc = jy * P.nc + wrap_cell(cx + sx, P.nc);
+      const int e = B.cell_off[jc + 1];
+      for (int j = B.cell_off[jc]; j < e; ++j)
+      {
+        if (j == q) continue;
+        const uint4 rj = rec[j];
+        const float dx = (float) (int) (rj.x - ri.x) * 2.3283064365386963e-10f;
+        const float dy = (float) (int) (rj.y - ri.y) * 2.3283064365386963e-10f;
+        if (fmaf(dx, dx, dy * dy) <= P.rmax2_f)
+        {
+          if (cnt < P.cap) B.vl[(long) cnt * P.n + q] = j;
+          ++cnt;
+        }
+      }
+    }
+  }
+  if (cnt > P.cap)
+  {
+    atomicMax(&B.ctrl->overflow, cnt);
+    cnt = -1;
+  }
+  B.vl_cnt[q] = cnt;
+}
+
+// ---------------------------------------------------------------- step
+
+template<int KIND>
+__device__ __forceinline__ void gather_sums(const FastParams &P, const FastBuffers &B, const uint4 *rec, const uint2 *lo,
+                                            int q, const uint4 &ri, uint64_t Xi, uint64_t Yi, Acc &a)
+{
+  if (KIND == KIND_VERLET)
+  {
+    const int cnt = B.vl_cnt[q];
+    if (cnt >= 0)
+    {
+      for (int m = 0; m < cnt; ++m)
+      {
+        const int j = B.vl[(long) m * P.n + q];
+        candidate(P, ri, Xi, Yi, __ldg(&rec[j]), lo, j, a);
+      }
+      return;
+    }
+    // list longer than the capacity: the stencil of the rebuild-time cell holds
+    // every particle the list would (displacements since the rebuild < skin / 2)
+  }
+  if (KIND == KIND_ALL_PAIRS)
+  {
+    for (int j = 0; j < P.n; ++j)
+      if (j != q) candidate(P, ri, Xi, Yi, __ldg(&rec[j]), lo, j, a);
+    return;
+  }
+  const int c = B.cell_sorted[q];
+  const int cx = c % P.nc, cy = c / P.nc;
+  // stencil in the reference's order (-1,-1),(0,-1),(1,-1),(-1,0),... (ParticleSystemFirstOrder.cpp:47-52)
+  for (int sy = -1; sy <= 1; ++sy)
+  {
+    const int jy = wrap_cell(cy + sy, P.nc);
+    for (int sx = -1; sx <= 1; ++sx)
+    {
+      const int jc = jy * P.nc + wrap_cell(cx + sx, P.nc);
+      const int e = B.cell_off[jc + 1];
+      for (int j = B.cell_off[jc]; j < e; ++j)
+        if (j != q) candidate(P, ri, Xi, Yi, __ldg(&rec[j]), lo, j, a);
+    }
+  }
+}
+
+// One SE or SRK step of one particle.  STEPPER: 1 stochastic Euler, 2 strong
+// order 1.5 Taylor.  Per-particle FP32 sums of sin/cos(phi_j - phi_i) and
+// omega_j sin/cos(phi_j - phi_i) give the alignment force and the
+// complementary force of the SRK scheme.
+template<int MODEL, int STEPPER, int KIND>
+__global__ void __launch_bounds__(kTB) fast_step_kernel(FastParams P, FastBuffers B)
+{
+  __shared__ float smax[kTB / 32];
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  FastControl *ctrl = B.ctrl;
+  const int par = ctrl->parity;
+  const uint4 *rin = par ? B.rec1 : B.rec0;
+  const uint2 *lin = par ? B.lo1 : B.lo0;
+  uint4 *rout = par ? B.rec0 : B.rec1;
+  uint2 *lout = par ? B.lo0 : B.lo1;
+  float d2max = 0.0f;
+  int err = 0;
+  if (q < P.n)
+  {
+    const uint4 ri = rin[q];
+    const uint2 li = lin[q];
+    const uint64_t Xi = join64(ri.x, li.x), Yi = join64(ri.y, li.y);
+    const float wi = __uint_as_float(ri.w);
+    Acc a{0.f, 0.f, 0.f, 0.f, 0};
+    gather_sums<KIND>(P, B, rin, lin, q, ri, Xi, Yi, a);
+    float sphi, cphi;
+    phase_sincos(ri.z, sphi, cphi);
+    // alignment: sum sin(phi_j - phi_i - alpha); complementary: sum (w_j - w_i) cos(phi_j - phi_i - alpha)
+    float f_w = 0.0f, C = 0.0f;  // SE/SRK zero-fill the derivative: an isolated particle keeps 0
+    if (a.card > 0)
+    {
+      const float inv = 1.0f / (float) a.card;
+      const float F = P.ca * a.ss - P.sa * a.sc;
+      f_w = -P.xi_phi * wi + P.sigma * F * inv;
+      if (STEPPER == 2)
+      {
+        const float G = P.ca * (a.wc - wi * a.sc) + P.sa * (a.ws - wi * a.ss);
+        C = P.sigma * inv * G;
+      }
+    }
+    const unsigned p = B.pid[q];
+    NoiseKey nk;
+    nk.seed = P.seed;
+    nk.replica = P.replica;
+    nk.step = ctrl->step;
+    float z[8];
+    normals4_f32(nk, p, 0, z);
+    if (STEPPER == 2 && MODEL == 2) normals4_f32(nk, p, 1, z + 4);
+    const float dt = P.dt;
+    float ddx, ddy, dphi, dw;
+    int2 im = B.img[q];
+    int turns = B.turns[q];
+    const int2 im0 = im;
+    const int turns0 = turns;
+    if (MODEL == 1)
+    {
+      const float fx = P.v0 * cphi, fy = P.v0 * sphi, fp = wi;
+      if (STEPPER == 1)
+      {
+        // StochasticEulerStepperPtr.hpp:58-66
+        ddx = fx * dt;
+        ddy = fy * dt;
+        dphi = fp * dt;
+        dw = f_w * dt + P.b_phi * (P.sqdt * z[0]);
+      } else
+      {
+        // StochasticRungeKuttaStepperPtr.hpp:54-70
+        const float dW = z[0] * P.sqdt;
+        const float dZ = P.half_dt15 * (z[0] + P.inv_sqrt3 * z[1]);
+        ddx = fx * dt - fp * fy * P.half_dt2;
+        ddy = fy * dt + fp * fx * P.half_dt2;
+        dphi = fp * dt + f_w * P.half_dt2 + P.b_phi * dZ;
+        dw = f_w * dt + (C - P.xi * f_w) * P.half_dt2 + P.b_phi * (dW - P.xi * dZ);
+      }
+    } else
+    {
+      const float2 v = B.vel[q];
+      const float fvx = -P.xi_r * v.x + P.v0 * cphi, fvy = -P.xi_r * v.y + P.v0 * sphi;
+      float dvx, dvy;
+      if (STEPPER == 1)
+      {
+        // StochasticEulerStepper.hpp:44-50 with AddNoise (ParticleSystemSecondOrder.cpp:447-449)
+        ddx = dt * v.x;
+        ddy = dt * v.y;
+        dvx = dt * fvx + P.sqdt * (P.b_r * z[0]);
+        dvy = dt * fvy + P.sqdt * (P.b_r * z[1]);
+        dphi = dt * wi;
+        dw = dt * f_w + P.sqdt * (P.b_phi * z[2]);
+      } else
+      {
+        // second-order strong order 1.5 Taylor scheme (no reference code)
+        const float dWx = z[0] * P.sqdt, dZx = P.half_dt15 * (z[0] + P.inv_sqrt3 * z[1]);
+        const float dWy = z[2] * P.sqdt, dZy = P.half_dt15 * (z[2] + P.inv_sqrt3 * z[3]);
+        const float dWw = z[4] * P.sqdt, dZw = P.half_dt15 * (z[4] + P.inv_sqrt3 * z[5]);
+        ddx = v.x * dt + fvx * P.half_dt2 + P.b_r * dZx;
+        ddy = v.y * dt + fvy * P.half_dt2 + P.b_r * dZy;
+        dvx = fvx * dt + (-P.xi_r * fvx - P.v0 * sphi * wi) * P.half_dt2 + P.b_r * (dWx - P.xi_r * dZx);
+        dvy = fvy * dt + (-P.xi_r * fvy + P.v0 * cphi * wi) * P.half_dt2 + P.b_r * (dWy - P.xi_r * dZy);
+        dphi = wi * dt + f_w * P.half_dt2 + P.b_phi * dZw;
+        dw = f_w * dt + (C - P.xi_phi * f_w) * P.half_dt2 + P.b_phi * (dWw - P.xi_phi * dZw);
+      }
+      B.vel[q] = make_float2(v.x + dvx, v.y + dvy);
+    }
+    const uint64_t Xn = advance(Xi, fix64_of(ddx, err), im.x);
+    const uint64_t Yn = advance(Yi, fix64_of(ddy, err), im.y);
+    const uint32_t Pn = advance_phase(ri.z, dphi, turns, err);
+    rout[q] = make_uint4((uint32_t) (Xn >> 32), (uint32_t) (Yn >> 32), Pn, __float_as_uint(wi + dw));
+    lout[q] = make_uint2((uint32_t) Xn, (uint32_t) Yn);
+    if (im.x != im0.x || im.y != im0.y) B.img[q] = im;
+    if (turns != turns0) B.turns[q] = turns;
+    d2max = fmaf(ddx, ddx, ddy * ddy);
+  }
+  // block max of |dr|^2 for the Verlet trigger
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) d2max = fmaxf(d2max, __shfl_xor_sync(0xffffffffu, d2max, off));
+  if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = d2max;
+  err = __syncthreads_or(err);
+  if (threadIdx.x < 32)
+  {
+    float m = threadIdx.x < kTB / 32 ? smax[threadIdx.x] : 0.0f;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+    if (threadIdx.x == 0)
+    {
+      atomicMax(&ctrl->max2_bits, __float_as_uint(m));
+      if (err) atomicOr(&ctrl->error, 1);
+    }
+  }
+}
+
+// After a step: advance the noise counter and the buffer parity, accumulate
+// the displacement in FP64 and set the rebuild flag
+// (CalculateMaxDisplacement, ParticleSystemFirstOrder.cpp:670-696).
+__global__ void fast_control_kernel(FastControl *ctrl, double half_skin, int always_rebuild, int verlet)
+{
+  ctrl->step += 1;
+  ctrl->parity ^= 1;
+  const double max2 = (double) __uint_as_float(ctrl->max2_bits);
+  ctrl->max2_bits = 0u;
+  if (always_rebuild)
+  {
+    ctrl->rebuild = 1;
+    return;
+  }
+  if (verlet)
+  {
+    ctrl->acc += sqrt(max2);
+    if (ctrl->acc > half_skin)
+    {
+      ctrl->acc = 0.0;
+      ctrl->rebuild = 1;
+    }
+  }
+}
+
+__global__ void fast_set_condition_kernel(const FastControl *ctrl, cudaGraphConditionalHandle handle)
+{
+  cudaGraphSetConditional(handle, ctrl->rebuild ? 1u : 0u);
+}
+
+__global__ void fast_noise_kernel(double *__restrict__ out, int n, int per, NoiseKey nk)
+{
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  float z[8];
+  normals4_f32(nk, (uint32_t) p, 0, z);
+  if (per > 4) normals4_f32(nk, (uint32_t) p, 1, z + 4);
+  for (int d = 0; d < per; ++d) out[(long) per * p + d] = (double) z[d];
+}
+
+// ApplyPeriodicBoundaryConditions: positions are kept wrapped; forget the box crossings.
+__global__ void fast_pbc_kernel(int2 *img, int n)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) img[q] = make_int2(0, 0);
+}
+
+// ---------------------------------------------------------------- host side
+
+static int blocks_for(long n, int tb)
+{
+  return (int) ((n + tb - 1) / tb);
+}
+
+static FastBuffers buffers(spss_ctx *ctx)
+{
+  FastPath *f = ctx->fast;
+  FastBuffers B;
+  B.rec0 = f->rec[0].ptr;
+  B.rec1 = f->rec[1].ptr;
+  B.lo0 = f->lo[0].ptr;
+  B.lo1 = f->lo[1].ptr;
+  B.vel = f->vel.ptr;
+  B.vel_tmp = f->vel_tmp.ptr;
+  B.pid = f->pid.ptr;
+  B.pid_tmp = f->pid_tmp.ptr;
+  B.img = f->img.ptr;
+  B.img_tmp = f->img_tmp.ptr;
+  B.turns = f->turns.ptr;
+  B.turns_tmp = f->turns_tmp.ptr;
+  B.cell_of = f->cell_of.ptr;
+  B.cell_sorted = f->cell_sorted.ptr;
+  B.cell_off = f->binner.offsets.ptr;
+  B.order = f->binner.members.ptr;
+  B.vl = f->vl.ptr;
+  B.vl_cnt = f->vl_cnt.ptr;
+  B.caf = f->caf.ptr;
+  B.ctrl = f->ctrl;
+  return B;
+}
+
+static FastParams params(spss_ctx *ctx, double dt)
+{
+  const spss_params &p = ctx->p;
+  FastPath *f = ctx->fast;
+  FastParams P;
+  std::memset(&P, 0, sizeof(P));
+  P.n = p.n;
+  P.nc = f->nc_build;
+  P.cap = f->cap;
+  P.model = p.model;
+  P.kind = f->kind;
+  P.always_rebuild = f->kind == KIND_CELLS ? 1 : 0;
+  P.v0 = (float) p.v0;
+  P.xi = (float) p.xi;
+  P.xi_r = (float) p.xi_r;
+  // first order: the torque friction is xi; second order: xi_phi
+  P.xi_phi = (float) (p.model == 1 ? p.xi : p.xi_phi);
+  P.sigma = (float) p.sigma;
+  P.ca = (float) std::cos(p.alpha);
+  P.sa = (float) std::sin(p.alpha);
+  const double rho2 = p.rho * p.rho;
+  P.rho2_d = rho2;
+  P.rho2_f = (float) rho2;
+  // |d2_f - d2| <= 2 (|dx| + |dy|) 2^-32 + 2^-32 + 4 d2 2^-24 near r = rho; doubled
+  P.band_f = (float) (2.0 * (4.0 * p.rho * 2.3283064365386963e-10 + 2.3283064365386963e-10 + 4.0 * rho2 * 5.9604644775390625e-8));
+  const double rmax2 = ctx->r_max * ctx->r_max;
+  P.rmax2_f = (float) (rmax2 + 2.0 * (4.0 * ctx->r_max * 2.3283064365386963e-10 + 4.0 * rmax2 * 5.9604644775390625e-8));
+  P.half_skin = 0.5 * (ctx->r_max - ctx->r_min);
+  P.dt = (float) dt;
+  P.sqdt = (float) std::sqrt(dt);
+  P.half_dt2 = (float) (0.5 * dt * dt);
+  P.half_dt15 = (float) (0.5 * std::pow(dt, 1.5));
+  P.inv_sqrt3 = (float) (1.0 / std::sqrt(3.0));
+  P.b_r = (float) std::sqrt(2.0 * p.D_r);
+  P.b_phi = (float) std::sqrt(2.0 * p.D_phi);
+  P.seed = p.seed;
+  P.replica = p.replica;
+  return P;
+}
+
+int fast_create(spss_ctx *ctx)
+{
+  FastPath *f = new FastPath();
+  ctx->fast = f;
+  const spss_params &p = ctx->p;
+  const int n = p.n;
+  const int variant = variant_for(ctx, p.variant);
+  switch (variant)
+  {
+    case SPSS_VARIANT_ALL_PAIRS:
+      f->kind = KIND_ALL_PAIRS;
+      f->nc_build = 1;
+      break;
+    case SPSS_VARIANT_LINKED_LIST:
+      f->kind = KIND_CELLS;
+      f->nc_build = ctx->nc;
+      break;
+    case SPSS_VARIANT_VERLET:
+      // O(N^2) list build = every pair within r_max: cells no smaller than r_max
+      f->kind = KIND_VERLET;
+      f->nc_build = std::max(1, (int) (1.0 / ctx->r_max));
+      if (f->nc_build < 3) return SPSS_ERR_NOT_SUPPORTED;
+      break;
+    case SPSS_VARIANT_LINKED_LIST_VERLET:
+      f->kind = KIND_VERLET;
+      f->nc_build = ctx->nc_verlet;
+      break;
+    default:
+      return SPSS_ERR_NOT_SUPPORTED;  // global field: FP64 contexts
+  }
+  if (f->kind == KIND_VERLET) ctx->uses_verlet_list = 1;
+  for (int b = 0; b < 2; ++b)
+  {
+    SPSS_TRY(f->rec[b].reserve(n));
+    SPSS_TRY(f->lo[b].reserve(n));
+  }
+  SPSS_TRY(f->vel.reserve(n));
+  SPSS_TRY(f->vel_tmp.reserve(n));
+  SPSS_TRY(f->pid.reserve(n));
+  SPSS_TRY(f->pid_tmp.reserve(n));
+  SPSS_TRY(f->img.reserve(n));
+  SPSS_TRY(f->img_tmp.reserve(n));
+  SPSS_TRY(f->turns.reserve(n));
+  SPSS_TRY(f->turns_tmp.reserve(n));
+  SPSS_TRY(f->cell_of.reserve(n));
+  SPSS_TRY(f->cell_sorted.reserve(n));
+  SPSS_TRY(f->caf.reserve(n));
+  SPSS_TRY(f->vl_cnt.reserve(n));
+  if (f->kind == KIND_VERLET)
+  {
+    // mean list length: pi r_max^2 n (unit box); room for six standard deviations
+    const double lam = M_PI * ctx->r_max * ctx->r_max * n;
+    f->cap = std::max(16, ((int) std::ceil(lam + 6.0 * std::sqrt(lam) + 8.0) + 3) & ~3);
+    SPSS_TRY(f->vl.reserve((size_t) f->cap * n));
+  }
+  SPSS_CUDA_TRY(cudaMalloc((void **) &f->ctrl, sizeof(FastControl)));
+  SPSS_CUDA_TRY(cudaMallocHost((void **) &f->h_ctrl, sizeof(FastControl)));
+  std::memset(f->h_ctrl, 0, sizeof(FastControl));
+  f->h_ctrl->rebuild = 1;
+  f->h_ctrl->uses_verlet = f->kind == KIND_VERLET;
+  SPSS_CUDA_TRY(cudaMemcpyAsync(f->ctrl, f->h_ctrl, sizeof(FastControl), cudaMemcpyHostToDevice, ctx->stream));
+  SPSS_CUDA_TRY(cudaMemsetAsync(f->vel.ptr, 0, sizeof(float2) * n, ctx->stream));
+  SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SPSS_OK;
+}
+
+void fast_destroy(spss_ctx *ctx)
+{
+  FastPath *f = ctx->fast;
+  if (!f) return;
+  for (auto &g : f->graphs)
+  {
+    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+    if (g.second.graph) cudaGraphDestroy(g.second.graph);
+  }
+  for (int b = 0; b < 2; ++b)
+  {
+    f->rec[b].release();
+    f->lo[b].release();
+  }
+  f->vel.release();
+  f->vel_tmp.release();
+  f->pid.release();
+  f->pid_tmp.release();
+  f->img.release();
+  f->img_tmp.release();
+  f->turns.release();
+  f->turns_tmp.release();
+  f->cell_of.release();
+  f->cell_sorted.release();
+  f->vl.release();
+  f->vl_cnt.release();
+  f->caf.release();
+  f->binner.release();
+  if (f->ctrl) cudaFree(f->ctrl);
+  if (f->h_ctrl) cudaFreeHost(f->h_ctrl);
+  delete f;
+  ctx->fast = nullptr;
+}
+
+// Cell binning, slot re-sort and (Verlet) list build, as one stream sequence.
+static int launch_rebuild(spss_ctx *ctx, const FastParams &P)
+{
+  FastPath *f = ctx->fast;
+  const FastBuffers B = buffers(ctx);
+  const int n = P.n;
+  if (f->kind != KIND_ALL_PAIRS)
+  {
+    fast_cells_kernel<<<blocks_for(n, kTB), kTB, 0, ctx->stream>>>(P, B);
+    ++ctx->launches;
+    SPSS_TRY(check_launch("fast_cells_kernel"));
+    SPSS_TRY(f->binner.run(f->cell_of.ptr, n, P.nc * P.nc, ctx->stream, ctx->launches));
+    const FastBuffers B2 = buffers(ctx);  // binner buffers exist now
+    fast_permute_kernel<<<blocks_for(n, kTB), kTB, 0, ctx->stream>>>(P, B2);
+    ++ctx->launches;
+    SPSS_TRY(check_launch("fast_permute_kernel"));
+    fast_copyback_kernel<<<blocks_for(n, kTB), kTB, 0, ctx->stream>>>(P, B2);
+    ++ctx->launches;
+    SPSS_TRY(check_launch("fast_copyback_kernel"));
+  }
+  fast_after_rebuild_kernel<<<1, 1, 0, ctx->stream>>>(f->ctrl, f->kind != KIND_ALL_PAIRS);
+  ++ctx->launches;
+  SPSS_TRY(check_launch("fast_after_rebuild_kernel"));
+  if (f->kind == KIND_VERLET)
+  {
+    fast_verlet_build_kernel<<<blocks_for(n, 128), 128, 0, ctx->stream>>>(P, buffers(ctx));
+    ++ctx->launches;
+    SPSS_TRY(check_launch("fast_verlet_build_kernel"));
+  }
+  return SPSS_OK;
+}
+
+template<int MODEL, int STEPPER>
+static void launch_step_kind(spss_ctx *ctx, const FastParams &P, const FastBuffers &B)
+{
+  const int grid = blocks_for(P.n, kTB);
+  switch (ctx->fast->kind)
+  {
+    case KIND_ALL_PAIRS: fast_step_kernel<MODEL, STEPPER, KIND_ALL_PAIRS><<<grid, kTB, 0, ctx->stream>>>(P, B); break;
+    case KIND_CELLS: fast_step_kernel<MODEL, STEPPER, KIND_CELLS><<<grid, kTB, 0, ctx->stream>>>(P, B); break;
+    default: fast_step_kernel<MODEL, STEPPER, KIND_VERLET><<<grid, kTB, 0, ctx->stream>>>(P, B); break;
+  }
+}
+
+static int launch_step(spss_ctx *ctx, int stepper, const FastParams &P)
+{
+  const FastBuffers B = buffers(ctx);
+  if (ctx->timing) SPSS_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
+  if (ctx->p.model == 1)
+  {
+    if (stepper == SPSS_STEPPER_STOCHASTIC_EULER) launch_step_kind<1, 1>(ctx, P, B);
+    else launch_step_kind<1, 2>(ctx, P, B);
+  } else
+  {
+    if (stepper == SPSS_STEPPER_STOCHASTIC_EULER) launch_step_kind<2, 1>(ctx, P, B);
+    else launch_step_kind<2, 2>(ctx, P, B);
+  }
+  ++ctx->launches;
+  SPSS_TRY(check_launch("fast_step_kernel"));
+  if (ctx->timing) SPSS_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
+  fast_control_kernel<<<1, 1, 0, ctx->stream>>>(ctx->fast->ctrl, P.half_skin, P.always_rebuild,
+                                                 ctx->fast->kind == KIND_VERLET);
+  ++ctx->launches;
+  return check_launch("fast_control_kernel");
+}
+
+static int sync_control(spss_ctx *ctx)
+{
+  FastPath *f = ctx->fast;
+  SPSS_CUDA_TRY(cudaMemcpyAsync(f->h_ctrl, f->ctrl, sizeof(FastControl), cudaMemcpyDeviceToHost, ctx->stream));
+  SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  ctx->step_counter = f->h_ctrl->step;
+  ctx->accumulated_displacement = f->h_ctrl->acc;
+  ctx->should_update_lists = f->h_ctrl->rebuild;
+  if (f->h_ctrl->error) return SPSS_ERR_NONFINITE;
+  return SPSS_OK;
+}
+
+// The host-side step counter and list flag (spss_set_step_counter,
+// spss_set_should_update_lists) win over the device copy.
+static int push_host_control(spss_ctx *ctx)
+{
+  FastPath *f = ctx->fast;
+  if (f->h_ctrl->step == ctx->step_counter && f->h_ctrl->rebuild == ctx->should_update_lists) return SPSS_OK;
+  f->h_ctrl->step = ctx->step_counter;
+  f->h_ctrl->rebuild = ctx->should_update_lists;
+  SPSS_CUDA_TRY(cudaMemcpyAsync(f->ctrl, f->h_ctrl, sizeof(FastControl), cudaMemcpyHostToDevice, ctx->stream));
+  return SPSS_OK;
+}
+
+int fast_set_state(spss_ctx *ctx, const double *d_aos)
+{
+  FastPath *f = ctx->fast;
+  fast_upload_kernel<<<blocks_for(ctx->p.n, kTB), kTB, 0, ctx->stream>>>(d_aos, ctx->p.n, ctx->s, ctx->p.model,
+                                                                        f->perm_valid ? 1 : 0, buffers(ctx));
+  ++ctx->launches;
+  SPSS_TRY(check_launch("fast_upload_kernel"));
+  f->perm_valid = true;
+  f->have_state = true;
+  return SPSS_OK;
+}
+
+int fast_get_state(spss_ctx *ctx, double *d_aos)
+{
+  fast_download_kernel<<<blocks_for(ctx->p.n, kTB), kTB, 0, ctx->stream>>>(d_aos, ctx->p.n, ctx->s, ctx->p.model,
+                                                                          buffers(ctx));
+  ++ctx->launches;
+  return check_launch("fast_download_kernel");
+}
+
+int fast_step(spss_ctx *ctx, int stepper, double t, double dt)
+{
+  (void) t;
+  FastPath *f = ctx->fast;
+  if (!f->have_state) return SPSS_ERR_INVALID_ARGUMENT;
+  if (stepper == SPSS_STEPPER_RK4) return SPSS_ERR_NOT_SUPPORTED;
+  const FastParams P = params(ctx, dt);
+  SPSS_TRY(push_host_control(ctx));
+  if (f->h_ctrl->rebuild) SPSS_TRY(launch_rebuild(ctx, P));
+  SPSS_TRY(launch_step(ctx, stepper, P));
+  const int rc = sync_control(ctx);
+  if (ctx->timing)
+  {
+    float ms = 0.0f;
+    SPSS_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    ctx->timing_ms += ms;
+    ctx->timing_count += 1;
+  }
+  return rc;
+}
+
+static int build_graph_on(spss_ctx *ctx, int stepper, const FastParams &P, GraphEntry &g,
+                          unsigned long long launches0);
+
+// One step as a graph: rebuild under a conditional node, then step + control.
+static int build_graph(spss_ctx *ctx, int stepper, double dt, GraphEntry &g)
+{
+  const FastParams P = params(ctx, dt);
+  const unsigned long long launches0 = ctx->launches;
+  const int timing = ctx->timing;
+  cudaStream_t work = ctx->stream;
+  ctx->timing = 0;
+  ctx->stream = ctx->own_stream;  // capture needs a non-legacy stream
+  int rc_all = build_graph_on(ctx, stepper, P, g, launches0);
+  ctx->stream = work;
+  ctx->timing = timing;
+  return rc_all;
+}
+
+static int build_graph_on(spss_ctx *ctx, int stepper, const FastParams &P, GraphEntry &g,
+                          unsigned long long launches0)
+{
+  FastPath *f = ctx->fast;
+  cudaGraph_t graph;
+  SPSS_CUDA_TRY(cudaGraphCreate(&graph, 0));
+  cudaGraphConditionalHandle handle;
+  SPSS_CUDA_TRY(cudaGraphConditionalHandleCreate(&handle, graph, 0, cudaGraphCondAssignDefault));
+  // node 1: copy the rebuild flag into the condition
+  SPSS_CUDA_TRY(cudaStreamBeginCaptureToGraph(ctx->stream, graph, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  fast_set_condition_kernel<<<1, 1, 0, ctx->stream>>>(f->ctrl, handle);
+  ++ctx->launches;
+  SPSS_CUDA_TRY(cudaStreamEndCapture(ctx->stream, &graph));
+  size_t nnodes = 0;
+  SPSS_CUDA_TRY(cudaGraphGetNodes(graph, nullptr, &nnodes));
+  std::vector<cudaGraphNode_t> nodes(nnodes);
+  SPSS_CUDA_TRY(cudaGraphGetNodes(graph, nodes.data(), &nnodes));
+  cudaGraphNode_t set_node = nodes.back();
+  // node 2: IF rebuild
+  // the struct holds a union with deleted constructors: zeroed raw storage
+  alignas(cudaGraphNodeParams) unsigned char cp_storage[sizeof(cudaGraphNodeParams)] = {};
+  cudaGraphNodeParams &cp = *reinterpret_cast<cudaGraphNodeParams *>(cp_storage);
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = handle;
+  cp.conditional.type = cudaGraphCondTypeIf;
+  cp.conditional.size = 1;
+  cudaGraphNode_t cond_node;
+  SPSS_CUDA_TRY(cudaGraphAddNode(&cond_node, graph, &set_node, nullptr, 1, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  SPSS_CUDA_TRY(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  const unsigned long long before_body = ctx->launches;
+  int rc = launch_rebuild(ctx, P);
+  g.per_rebuild = (int) (ctx->launches - before_body);
+  cudaGraph_t body_out = body;
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &body_out);
+  if (rc != SPSS_OK) return rc;
+  SPSS_CUDA_TRY(e);
+  // nodes 3-4: step and control
+  SPSS_CUDA_TRY(cudaStreamBeginCaptureToGraph(ctx->stream, graph, &cond_node, nullptr, 1, cudaStreamCaptureModeRelaxed));
+  rc = launch_step(ctx, stepper, P);
+  e = cudaStreamEndCapture(ctx->stream, &graph);
+  if (rc != SPSS_OK) return rc;
+  SPSS_CUDA_TRY(e);
+  SPSS_CUDA_TRY(cudaGraphInstantiate(&g.exec, graph, 0));
+  g.graph = graph;
+  g.per_step = (int) (ctx->launches - launches0) - g.per_rebuild;
+  ctx->launches = launches0;  // captured, not launched
+  return SPSS_OK;
+}
+
+int fast_steps(spss_ctx *ctx, int stepper, double t0, double dt, int nsteps)
+{
+  (void) t0;
+  FastPath *f = ctx->fast;
+  if (!f->have_state) return SPSS_ERR_INVALID_ARGUMENT;
+  if (stepper == SPSS_STEPPER_RK4) return SPSS_ERR_NOT_SUPPORTED;
+  if (nsteps == 0) return SPSS_OK;
+  if (ctx->timing)
+  {
+    for (int k = 0; k < nsteps; ++k) SPSS_TRY(fast_step(ctx, stepper, t0 + (k + 1) * dt, dt));
+    return SPSS_OK;
+  }
+  SPSS_TRY(push_host_control(ctx));
+  // the first step runs eagerly so every lazily sized buffer exists before capture
+  if (!f->binner.offsets.ptr && f->kind != KIND_ALL_PAIRS)
+  {
+    SPSS_TRY(fast_step(ctx, stepper, t0 + dt, dt));
+    --nsteps;
+    if (nsteps == 0) return SPSS_OK;
+  }
+  auto key = std::make_pair(stepper, dt);
+  auto it = f->graphs.find(key);
+  if (it == f->graphs.end())
+  {
+    GraphEntry g;
+    SPSS_TRY(build_graph(ctx, stepper, dt, g));
+    it = f->graphs.emplace(key, g).first;
+  }
+  const int rebuilds0 = f->h_ctrl->rebuilds;
+  for (int k = 0; k < nsteps; ++k) SPSS_CUDA_TRY(cudaGraphLaunch(it->second.exec, ctx->stream));
+  const int rc = sync_control(ctx);
+  ctx->launches += (unsigned long long) nsteps * it->second.per_step
+      + (unsigned long long) (f->h_ctrl->rebuilds - rebuilds0) * it->second.per_rebuild;
+  return rc;
+}
+
+int fast_noise(spss_ctx *ctx, int stepper, unsigned long long step, double *d_out)
+{
+  const int per = normals_per_particle(ctx->p.model, stepper);
+  if (per == 0) return SPSS_OK;
+  NoiseKey nk;
+  nk.seed = ctx->p.seed;
+  nk.replica = ctx->p.replica;
+  nk.step = step;
+  fast_noise_kernel<<<blocks_for(ctx->p.n, kTB), kTB, 0, ctx->stream>>>(d_out, ctx->p.n, per, nk);
+  ++ctx->launches;
+  return check_launch("fast_noise_kernel");
+}
+
+int fast_evaluate(spss_ctx *, int, const double *, const double *, double *, double, double)
+{
+  return SPSS_ERR_NOT_SUPPORTED;
+}
+
+int fast_complementary_force(spss_ctx *, double *)
+{
+  return SPSS_ERR_NOT_SUPPORTED;
+}
+
+int fast_apply_pbc(spss_ctx *ctx)
+{
+  fast_pbc_kernel<<<blocks_for(ctx->p.n, kTB), kTB, 0, ctx->stream>>>(ctx->fast->img.ptr, ctx->p.n);
+  ++ctx->launches;
+  return check_launch("fast_pbc_kernel");
+}
+
 }  // namespace spss

@@ -177,10 +177,17 @@ int spss_create(const spss_params *params, spss_ctx **out)
   ctx->nc_verlet = p.nc_verlet > 0 ? p.nc_verlet : ctx->nc;
   ctx->should_update_lists = 1;
   int rc = SPSS_OK;
-  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess)
   {
     cudaGetLastError();
     delete ctx;
+    return SPSS_ERR_CUDA;
+  }
+  ctx->stream = ctx->own_stream;
+  if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess)
+  {
+    cudaGetLastError();
+    spss_destroy(ctx);
     return SPSS_ERR_CUDA;
   }
   rc = is_f64(ctx) ? f64_create(ctx) : fast_create(ctx);
@@ -204,7 +211,9 @@ int spss_destroy(spss_ctx *ctx)
   ctx->scratch_c.release();
   ctx->average.release();
   if (ctx->registered_host) cudaHostUnregister(ctx->registered_host);
-  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   cudaGetLastError();
   delete ctx;
   return SPSS_OK;
@@ -536,6 +545,31 @@ int spss_kernel_launches(spss_ctx *ctx, unsigned long long *count)
 {
   if (!ctx || !count) return SPSS_ERR_INVALID_ARGUMENT;
   *count = ctx->launches;
+  return SPSS_OK;
+}
+
+int spss_set_stream(spss_ctx *ctx, void *cuda_stream)
+{
+  if (!ctx) return SPSS_ERR_INVALID_ARGUMENT;
+  SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  ctx->stream = cuda_stream ? (cudaStream_t) cuda_stream : ctx->own_stream;
+  return SPSS_OK;
+}
+
+int spss_set_timing(spss_ctx *ctx, int on)
+{
+  if (!ctx) return SPSS_ERR_INVALID_ARGUMENT;
+  ctx->timing = on ? 1 : 0;
+  ctx->timing_ms = 0.0;
+  ctx->timing_count = 0;
+  return SPSS_OK;
+}
+
+int spss_get_timing(spss_ctx *ctx, double *kernel_ms, unsigned long long *timed_launches)
+{
+  if (!ctx) return SPSS_ERR_INVALID_ARGUMENT;
+  if (kernel_ms) *kernel_ms = ctx->timing_ms;
+  if (timed_launches) *timed_launches = ctx->timing_count;
   return SPSS_OK;
 }
 

@@ -208,7 +208,13 @@ struct spss_ctx
 {
   spss_params p{};
   int s = 4;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;      // where work is issued
+  cudaStream_t own_stream = nullptr;  // created with the context; graph capture runs here
+  // CUDA-event timing of the pair-and-update kernel (spss_set_timing)
+  int timing = 0;
+  double timing_ms = 0.0;
+  unsigned long long timing_count = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   unsigned long long launches = 0;
   unsigned long long step_counter = 0;
   int higher_order = 0;

@@ -1,0 +1,186 @@
+"""GB300 fast path (fixed-point positions, FP32 pair and stage arithmetic)
+against the FP64 oracle on identical noise (the oracle replays the normals the
+GPU drew), plus size-independent properties at the benchmark sizes.
+
+Tolerances (stated here, checked below):
+  * one step from the same FP64 state: every component within 1e-5 relative
+    (floor: 1e-5 of the component's largest magnitude); the step increments
+    themselves within 2e-4 of the component's largest increment;
+  * 50 steps: 99.9% of particles within 1e-3 relative (a neighbour crossing
+    the cutoff earlier or later on the diverging FP32 trajectory moves single
+    particles by more, as it would between two FP64 codes with different
+    summation orders);
+  * neighbour sets: exact (cutoff decisions inside an FP32 guard band are
+    recomputed in FP64 from the 64-bit fixed-point positions).
+"""
+import numpy as np
+import pytest
+
+from helpers import gpu_context, min_image, oracle_system
+
+pytestmark = pytest.mark.gpu
+
+F32 = 1
+
+
+def initial(model, n, seed, v=0.01, omega=0.5):
+    rng = np.random.default_rng(seed)
+    s = 4 if model == 1 else 6
+    x = np.zeros((n, s))
+    x[:, 0], x[:, 1] = rng.random(n), rng.random(n)
+    phi = rng.uniform(-np.pi, np.pi, n)
+    if model == 1:
+        x[:, 2], x[:, 3] = phi, rng.uniform(-omega, omega, n)
+    else:
+        x[:, 2], x[:, 3] = v * np.cos(phi), v * np.sin(phi)
+        x[:, 4], x[:, 5] = phi, rng.uniform(-omega, omega, n)
+    return x.reshape(-1)
+
+
+def params(model, n, density=2.0, R=1.0, v0=0.5, m=1.0, D=0.1, sigma=1.0, alpha=0.0):
+    """Physical parameters mapped to the reference's unit box (L = sqrt(N/density))."""
+    L = np.sqrt(n / density)
+    p = dict(model=model, n=n, rho=R / L, flavor="ptr", v0=v0 / L, sigma=sigma / m, alpha=alpha)
+    if model == 1:
+        p.update(xi=0.1, D_phi=D)
+    else:
+        p.update(xi_r=1.0 / m, xi_phi=1.0 / m, D_r=1e-3 / L ** 2, D_phi=D / m ** 2)
+    return p
+
+
+def state_err(got, ref, s):
+    got, ref = got.reshape(-1, s), ref.reshape(-1, s)
+    d = got - ref
+    d[:, :2] = min_image(d[:, :2])
+    scale = np.abs(ref).max(axis=0)
+    scale[:2] = 1.0
+    return np.abs(d) / (np.abs(ref) + scale)
+
+
+def run_pair(model, variant, stepper, n, steps, seed=3, skin=0.3, **kw):
+    p = params(model, n, **kw)
+    x0 = initial(model, n, seed, v=p["v0"])
+    r_max = (1.0 + skin) * p["rho"]
+    nc_v = int(1.0 / r_max)
+    ctx = gpu_context(p, precision=F32, variant=variant, r_max=r_max, nc_verlet=nc_v, seed=11)
+    orc = oracle_system(p, r_max=r_max, nc_verlet=nc_v)
+    ctx.set_state(x0)
+    x = x0.copy()
+    t, dt = 0.0, 0.005
+    for k in range(steps):
+        t += dt
+        normals = ctx.noise(stepper, k)
+        ctx.step(stepper, t, dt)
+        orc.step(stepper, variant, x, t, dt, normals)
+    got = ctx.get_state()
+    ctx.close()
+    return x0, got, x
+
+
+CASES = [(2, 2, 1), (2, 2, 2), (2, 4, 1), (2, 4, 2), (2, 1, 2), (1, 4, 2), (1, 2, 1), (1, 4, 1)]
+
+
+@pytest.mark.parametrize("model,variant,stepper", CASES)
+def test_one_step_matches_fp64_oracle(model, variant, stepper):
+    n = 400 if variant == 1 else 8192
+    x0, got, ref = run_pair(model, variant, stepper, n, 1)
+    s = 4 if model == 1 else 6
+    assert state_err(got, ref, s).max() <= 1e-5
+    inc_got, inc_ref = (got - x0).reshape(-1, s), (ref - x0).reshape(-1, s)
+    inc_got[:, :2], inc_ref[:, :2] = min_image(inc_got[:, :2]), min_image(inc_ref[:, :2])
+    for c in range(s):
+        scale = np.abs(inc_ref[:, c]).max()
+        assert np.abs(inc_got[:, c] - inc_ref[:, c]).max() <= 2e-4 * scale + 1e-12, c
+
+
+@pytest.mark.parametrize("model,variant,stepper", [(2, 4, 2), (2, 2, 1), (1, 4, 2)])
+def test_fifty_steps_track_fp64_oracle(model, variant, stepper):
+    x0, got, ref = run_pair(model, variant, stepper, 4096, 50)
+    s = 4 if model == 1 else 6
+    err = state_err(got, ref, s).max(axis=1)
+    assert np.quantile(err, 0.999) <= 1e-3
+    assert np.median(err) <= 1e-5
+
+
+def test_isolated_particle_torque_derivative_is_zero_like_reference():
+    """SE/SRK zero-fill the derivative, so a particle without neighbours gets
+    omega += noise only (StochasticEulerStepper.hpp:36, StochasticRungeKuttaStepperPtr.hpp:43)."""
+    x0, got, ref = run_pair(2, 2, 1, 200, 1, density=0.05)  # sparse: many isolated particles
+    assert state_err(got, ref, 6).max() <= 1e-5
+
+
+def test_graph_steps_equal_single_steps_bitwise():
+    p = params(2, 20000)
+    x0 = initial(2, 20000, 5, v=p["v0"])
+    r_max = 1.3 * p["rho"]
+    out = []
+    for use_graph in (False, True):
+        with gpu_context(p, precision=F32, variant=4, r_max=r_max, nc_verlet=int(1 / r_max), seed=3) as ctx:
+            ctx.set_state(x0)
+            if use_graph:
+                ctx.steps(2, 0.0, 0.005, 120)
+            else:
+                for k in range(120):
+                    ctx.step(2, (k + 1) * 0.005, 0.005)
+            out.append((ctx.get_state(), ctx.verlet_state(), ctx.step_counter))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    assert out[0][1] == out[1][1]
+    assert out[0][2] == out[1][2] == 120
+
+
+def test_verlet_equals_linked_list_at_benchmark_size():
+    """Config-3 size: the Verlet path (skin 0.3 R, rebuilt on the displacement
+    trigger) and the per-step cell list see the same neighbour sets, so the
+    trajectories agree to FP32 summation-order differences."""
+    n = 4194304
+    p = params(2, n)
+    x0 = initial(2, n, 9, v=p["v0"])
+    r_max = 1.3 * p["rho"]
+    res = {}
+    for variant in (2, 4):
+        with gpu_context(p, precision=F32, variant=variant, r_max=r_max, nc_verlet=int(1 / r_max), seed=5) as ctx:
+            ctx.set_state(x0)
+            ctx.steps(2, 0.0, 0.005, 20)
+            res[variant] = ctx.get_state()
+            assert np.all(np.isfinite(res[variant]))
+    err = state_err(res[4], res[2], 6).max(axis=1)
+    assert np.quantile(err, 0.9999) <= 1e-4
+
+
+def test_step_host_matches_device_steps():
+    p = params(2, 5000)
+    x0 = initial(2, 5000, 2, v=p["v0"])
+    with gpu_context(p, precision=F32, variant=2, seed=8) as a, gpu_context(p, precision=F32, variant=2, seed=8) as b:
+        a.set_state(x0)
+        host = x0.copy()
+        for k in range(5):
+            a.step(1, (k + 1) * 0.005, 0.005)
+            b.step_host(1, host, (k + 1) * 0.005, 0.005)
+        np.testing.assert_array_equal(a.get_state(), host)
+
+
+def test_upload_download_round_trip():
+    p = params(2, 3000)
+    x0 = initial(2, 3000, 4, v=p["v0"])
+    x0[::6] += 3.0  # positions outside the box keep their image
+    x0[4::6] += 25.0  # phases beyond 2 pi keep their turns
+    with gpu_context(p, precision=F32, variant=2) as ctx:
+        ctx.set_state(x0)
+        back = ctx.get_state().reshape(-1, 6)
+        ref = x0.reshape(-1, 6)
+        np.testing.assert_allclose(back[:, :2], ref[:, :2], rtol=0, atol=1e-15 * 8)
+        np.testing.assert_allclose(back[:, 4], ref[:, 4], rtol=0, atol=1e-8)
+        np.testing.assert_allclose(back[:, [2, 3, 5]], ref[:, [2, 3, 5]], rtol=1e-7)
+
+
+def test_deterministic_and_noise_reproducible():
+    p = params(2, 10000)
+    x0 = initial(2, 10000, 6, v=p["v0"])
+    r_max = 1.3 * p["rho"]
+    outs = []
+    for _ in range(2):
+        with gpu_context(p, precision=F32, variant=4, r_max=r_max, nc_verlet=int(1 / r_max), seed=21) as ctx:
+            ctx.set_state(x0)
+            ctx.steps(2, 0.0, 0.005, 30)
+            outs.append(ctx.get_state())
+    np.testing.assert_array_equal(outs[0], outs[1])
