@@ -230,6 +230,7 @@ def run_ours(args, rank, world, local_rank):
     import torch
 
     from spsslangevinintegration_gb300 import PRECISION_F32, Context, LINKED_LIST_VERLET
+    from spsslangevinintegration_gb300.replicas import max_over_ranks
 
     torch.cuda.set_device(local_rank)
     dist = None
@@ -266,12 +267,8 @@ def run_ours(args, rank, world, local_rank):
         e1.record(stream)
         barrier()
     t += DT * args.steps
-    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(e0.elapsed_time(e1))
     launches = ctx.kernel_launches - launches0
-    if dist is not None:
-        tm = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
-        ms = float(tm.item())
     value = world * n * args.steps / (ms * 1e-3)
 
     # roofline: the pair-and-update kernel alone, CUDA events on the same stream
@@ -297,11 +294,7 @@ def run_ours(args, rank, world, local_rank):
         ctx.step_host(SRK, host, t, DT)
         t += DT
     barrier()
-    e2e_s = time.perf_counter() - w0
-    if dist is not None:
-        tm = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
-        e2e_s = float(tm.item())
+    e2e_s = max_over_ranks(time.perf_counter() - w0)
     e2e_value = world * n * e2e_steps / e2e_s
     acc, flag, uses = ctx.verlet_state()
     ctx.close()

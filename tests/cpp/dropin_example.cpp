@@ -1,0 +1,84 @@
+// Uses the drop-in classes exactly as the reference's engines use theirs
+// (ControlEngines/SimulationEngineSecondOrder.cpp:122-143): construct
+// Thread, PeriodicBoundaryConditions, a particle system and a stepper, then
+// call DoStep in a loop.  Built and run by tests/test_gpu_dropin.py, which
+// checks the written states against the oracle.
+//
+// usage: dropin_example <dir>   reads <dir>/fo_init.bin, <dir>/so_init.bin
+//                                writes fo_final.bin, so_final.bin, so_noise.bin
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "spss/spss.hpp"
+
+static std::vector<Real> read_all(const std::string &path, size_t n)
+{
+  std::vector<Real> v(n);
+  FILE *f = std::fopen(path.c_str(), "rb");
+  if (!f || std::fread(v.data(), sizeof(Real), n, f) != n) throw std::runtime_error("read " + path);
+  std::fclose(f);
+  return v;
+}
+
+static void write_all(const std::string &path, const std::vector<Real> &v)
+{
+  FILE *f = std::fopen(path.c_str(), "wb");
+  std::fwrite(v.data(), sizeof(Real), v.size(), f);
+  std::fclose(f);
+}
+
+int main(int argc, char **argv)
+{
+  if (argc < 2) return 2;
+  const std::string dir = argv[1];
+  try
+  {
+    {
+      // first order, serial class, RK4, rho = 0.1 -> linked list + Verlet by the reference's dispatch
+      const int n = 400, s = 4;
+      Thread thread(argc, argv, n, s);
+      PeriodicBoundaryConditions pbc(&thread, n, s, 1.0, 1.0);
+      ParticleSystemFirstOrder system(&thread, 0.3, 0.1, 1.0, 0.1, 0.2, 0.1, pbc, n, s);
+      RungeKutta4Stepper stepper(&thread, n, s);
+      std::vector<Real> x = read_all(dir + "/fo_init.bin", (size_t) n * s);
+      Real t = 0.0, dt = 0.01;
+      for (int k = 0; k < 10; ++k)
+      {
+        t += dt;
+        stepper.DoStep(system, x, t, dt);
+      }
+      write_all(dir + "/fo_final.bin", x);
+      if (!system.uses_verlet_list_) throw std::runtime_error("uses_verlet_list_ not set");
+    }
+    {
+      // second order, serial class, stochastic Euler, linked list; noise of each step recorded
+      const int n = 500, s = 6;
+      Thread thread(argc, argv, n, s);
+      PeriodicBoundaryConditions pbc(&thread, n, s, 1.0, 1.0);
+      ParticleSystemSecondOrder system(&thread, 0.5, 1.0, 0.02, 1.0, 0.1, 1.0, 0.07, 0.0, pbc, n, s);
+      StochasticEulerStepper stepper(&thread, n, s);
+      std::vector<Real> x = read_all(dir + "/so_init.bin", (size_t) n * s);
+      std::vector<Real> noise;
+      Real t = 0.0, dt = 0.005;
+      for (int k = 0; k < 5; ++k)
+      {
+        std::vector<Real> z((size_t) n * 3);
+        spss::check(spss_noise(system.context(), SPSS_STEPPER_STOCHASTIC_EULER, (unsigned long long) k, z.data(),
+                               (long) z.size()), "spss_noise");
+        noise.insert(noise.end(), z.begin(), z.end());
+        t += dt;
+        stepper.DoStep(system, x, t, dt);
+        pbc.ApplyPeriodicBoundaryConditions(x);
+      }
+      write_all(dir + "/so_final.bin", x);
+      write_all(dir + "/so_noise.bin", noise);
+    }
+  } catch (const std::exception &e)
+  {
+    std::fprintf(stderr, "dropin_example: %s\n", e.what());
+    return 1;
+  }
+  std::printf("ok\n");
+  return 0;
+}
