@@ -147,6 +147,28 @@ int spss_set_stream(spss_ctx *ctx, void *cuda_stream);
 int spss_set_timing(spss_ctx *ctx, int on);
 int spss_get_timing(spss_ctx *ctx, double *kernel_ms, unsigned long long *timed_launches);
 
+/* Largest particle count spss_order_parameters_noalloc accepts. */
+#define SPSS_NOALLOC_MAX_PARTICLES (1L << 30)
+
+/* The order parameters of spss_order_parameters, computed without allocating
+ * anything: for callers that must not call cudaMalloc, for instance code that
+ * runs while a CUDA graph is being captured (an allocation there breaks the
+ * capture) or a real-time loop in which cudaMalloc's implicit device
+ * synchronisation would stall.  No counterpart in the reference.
+ *
+ * `state` is a device array of the reference's AoS layout (n*4 or n*6
+ * doubles for model 1 or 2), `out4` a device array of 4 doubles that receives
+ * {|<e^{i phi}>|, arg, |<v/|v|>|, arg}; both belong to the caller.  The work
+ * is queued on `cuda_stream` (NULL: the legacy default stream) and nothing is
+ * synchronised.  The reduction's scratch is a fixed 32 KiB array inside the
+ * library (1024 block partials), held on every GPU that loads the library
+ * until the process exits and shared by all calls: calls that overlap on the
+ * GPU race on it; each call rewrites every partial it reads, so nothing needs
+ * clearing between calls.  The first call on a device looks up the array's
+ * device address, so make that first call before any stream capture.  Returns
+ * SPSS_ERR_SIZE for n <= 0 or n > SPSS_NOALLOC_MAX_PARTICLES. */
+int spss_order_parameters_noalloc(int model, const double *state, long n, double *out4, void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

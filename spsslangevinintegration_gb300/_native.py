@@ -89,6 +89,8 @@ SIGNATURES = {
     "spss_set_stream": (_i, [_vp, _vp]),
     "spss_set_timing": (_i, [_vp, _i]),
     "spss_get_timing": (_i, [_vp, _dp, P(_ull)]),
+    # device pointers in, device pointer out, caller's stream
+    "spss_order_parameters_noalloc": (_i, [_i, _vp, _l, _vp, _vp]),
 }
 
 

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <new>
 
 #include "spss_internal.cuh"
@@ -121,6 +122,38 @@ __global__ void accumulate_kernel(double *__restrict__ acc, const double *__rest
 {
   const long q = (long) blockIdx.x * blockDim.x + threadIdx.x;
   if (q < len) acc[q] += x[q];
+}
+
+// ------------------------------------------------ allocation-free order parameters
+//
+// Scratch of spss_order_parameters_noalloc: the per-block partial sums of one
+// call (kNoallocBlocks blocks x 4 sums, 32 KiB).  It lives in the library's
+// module, so every GPU that loads the library holds it until the process
+// exits, and every call shares it.  Each call overwrites the partials of all
+// blocks it reads, so nothing has to start at zero; calls that overlap on the
+// GPU (two streams at once) race on it.
+constexpr int kNoallocBlocks = 1024;
+static __device__ __align__(256) double g_noalloc_partials[kNoallocBlocks * 4];
+constexpr int kNoallocMaxDevices = 64;
+static double *g_noalloc_address[kNoallocMaxDevices];
+static std::mutex g_noalloc_mutex;
+
+// Device address of the scratch on the current device, looked up once per
+// device (host code cannot use the symbol itself: it names a host stand-in).
+static int noalloc_scratch(double **out)
+{
+  int dev = 0;
+  SPSS_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoallocMaxDevices) return SPSS_ERR_NOT_SUPPORTED;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_address[dev])
+  {
+    void *p = nullptr;
+    SPSS_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_partials));
+    g_noalloc_address[dev] = static_cast<double *>(p);
+  }
+  *out = g_noalloc_address[dev];
+  return SPSS_OK;
 }
 
 }  // namespace spss
@@ -546,6 +579,21 @@ int spss_kernel_launches(spss_ctx *ctx, unsigned long long *count)
   if (!ctx || !count) return SPSS_ERR_INVALID_ARGUMENT;
   *count = ctx->launches;
   return SPSS_OK;
+}
+
+int spss_order_parameters_noalloc(int model, const double *state, long n, double *out4, void *cuda_stream)
+{
+  if ((model != 1 && model != 2) || !state || !out4) return SPSS_ERR_INVALID_ARGUMENT;
+  if (n <= 0 || n > SPSS_NOALLOC_MAX_PARTICLES) return SPSS_ERR_SIZE;
+  double *partials = nullptr;
+  SPSS_TRY(noalloc_scratch(&partials));
+  const int s = model == 1 ? 4 : 6;
+  const int nparts = (int) std::min<long>(kNoallocBlocks, (n + 255) / 256);
+  cudaStream_t stream = (cudaStream_t) cuda_stream;
+  order_partials_kernel<<<nparts, 256, 0, stream>>>(state, (int) n, s, model, partials);
+  SPSS_TRY(check_launch("order_partials_kernel"));
+  order_finish_kernel<<<1, 32, 0, stream>>>(partials, nparts, (int) n, model, out4);
+  return check_launch("order_finish_kernel");
 }
 
 int spss_set_stream(spss_ctx *ctx, void *cuda_stream)
