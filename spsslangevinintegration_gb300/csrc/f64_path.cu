@@ -620,7 +620,7 @@ void f64_destroy(spss_ctx *ctx)
 int f64_set_state(spss_ctx *ctx, const double *d_aos)
 {
   const long len = (long) ctx->p.n * ctx->s;
-  SPSS_CUDA_TRY(cudaMemcpyAsync(ctx->f64->state.ptr, d_aos, sizeof(double) * len, cudaMemcpyDeviceToDevice,
+  SPSS_CUDA_TRY(cudaMemcpyAsync(ctx->f64->state.ptr, d_aos, sizeof(double) * len, cudaMemcpyDefault,
                                 ctx->stream));
   return SPSS_OK;
 }
@@ -628,7 +628,7 @@ int f64_set_state(spss_ctx *ctx, const double *d_aos)
 int f64_get_state(spss_ctx *ctx, double *d_aos)
 {
   const long len = (long) ctx->p.n * ctx->s;
-  SPSS_CUDA_TRY(cudaMemcpyAsync(d_aos, ctx->f64->state.ptr, sizeof(double) * len, cudaMemcpyDeviceToDevice,
+  SPSS_CUDA_TRY(cudaMemcpyAsync(d_aos, ctx->f64->state.ptr, sizeof(double) * len, cudaMemcpyDefault,
                                 ctx->stream));
   return SPSS_OK;
 }

@@ -2,14 +2,18 @@
 // fused pair sums + stochastic stepper update + Philox noise.
 //
 // Representation (slot order; slots are re-sorted by cell at every rebuild):
-//   rec[2][n]  uint4 {x_hi, y_hi, phase, omega bits}  double-buffered: a step
-//              reads rec[parity] (neighbours see the previous state) and
-//              writes rec[parity ^ 1]
-//   lo[2][n]   uint2 {x_lo, y_lo}, double-buffered with rec
-//   vel[n]     float2 {v_x, v_y} (second-order model)
-//   pid[n]     original particle index (noise counter, output order)
-//   img[n]     int2 box crossings since upload; turns[n] 2*pi turns of phase
+//   rec[2][n]  uint4 {x_hi, y_hi, cos phi, sin phi}: the record a neighbour
+//              gathers; double-buffered, a step reads rec[parity] (neighbours
+//              see the previous state) and writes rec[parity ^ 1]
+//   aux[2][n]  uint4 {x_lo, y_lo, phase, omega}, double-buffered with rec
+//   vel[n]     float2 {v_x, v_y} (second-order model), updated in place
+//   pid[n]     original particle index (noise counter, output order); inv[n]
+//              its inverse; img[n] box crossings; turns[n] 2*pi turns of phase
 // x = img + (x_hi * 2^32 + x_lo) * 2^-64 (unit box), phase = 2*pi*(turns + phase * 2^-32).
+//
+// The owner of a particle evaluates cos and sin of its phase once per step and
+// stores them in its record, so a pair costs no transcendental:
+// sum_j sin(phi_j - phi_i) = cos phi_i sum_j sin phi_j - sin phi_i sum_j cos phi_j.
 //
 // FP64 appears only where the result must not depend on FP32 rounding: the
 // exact cutoff decision inside a guard band around r = rho (a few pairs per
@@ -38,7 +42,7 @@ struct FastControl
 {
   unsigned long long step;  // Philox step counter of the next stochastic step
   double acc;               // accumulated displacement (FP64)
-  int parity;               // current rec/lo buffer
+  int parity;               // current rec/aux buffer
   int rebuild;              // lists (and slot order) rebuilt before the next evaluation
   unsigned int max2_bits;   // max |dr|^2 of the step, FP32 bits (non-negative floats order as ints)
   int overflow;             // largest Verlet count seen beyond capacity (0: none)
@@ -70,16 +74,16 @@ struct FastParams
 struct FastBuffers
 {
   uint4 *rec0, *rec1;
-  uint2 *lo0, *lo1;
+  uint4 *aux0, *aux1;
   float2 *vel, *vel_tmp;
-  unsigned *pid, *pid_tmp;
+  unsigned *pid, *pid_tmp, *inv;
   int2 *img, *img_tmp;
   int *turns, *turns_tmp;
   int *cell_of, *cell_sorted;
   const int *cell_off;
   const int *order;
-  int *vl, *vl_cnt;
-  float *caf;
+  short *vl;
+  int *vl_cnt;
   FastControl *ctrl;
 };
 
@@ -93,13 +97,12 @@ struct GraphEntry
 
 struct FastPath
 {
-  DeviceArray<uint4> rec[2];
-  DeviceArray<uint2> lo[2];
+  DeviceArray<uint4> rec[2], aux[2];
   DeviceArray<float2> vel, vel_tmp;
-  DeviceArray<unsigned> pid, pid_tmp;
+  DeviceArray<unsigned> pid, pid_tmp, inv;
   DeviceArray<int2> img, img_tmp;
-  DeviceArray<int> turns, turns_tmp, cell_of, cell_sorted, vl, vl_cnt;
-  DeviceArray<float> caf;
+  DeviceArray<int> turns, turns_tmp, cell_of, cell_sorted, vl_cnt;
+  DeviceArray<short> vl;
   Binner binner;
   FastControl *ctrl = nullptr;    // device
   FastControl *h_ctrl = nullptr;  // pinned mirror
@@ -188,8 +191,8 @@ struct Acc
 // image by integer subtraction); inside the guard band the decision is
 // recomputed in FP64 from the full 64-bit positions, so it equals the FP64
 // decision for these positions.
-__device__ __forceinline__ void candidate(const FastParams &P, const uint4 &ri, uint64_t Xi, uint64_t Yi,
-                                          const uint4 &rj, const uint2 *lo, int j, Acc &a)
+__device__ __forceinline__ bool in_range(const FastParams &P, const uint4 &ri, uint64_t Xi, uint64_t Yi,
+                                         const uint4 &rj, const uint4 *__restrict__ aux, int j)
 {
   const float dx = (float) (int) (rj.x - ri.x) * 2.3283064365386963e-10f;
   const float dy = (float) (int) (rj.y - ri.y) * 2.3283064365386963e-10f;
@@ -197,37 +200,111 @@ __device__ __forceinline__ void candidate(const FastParams &P, const uint4 &ri, 
   bool in = d2 <= P.rho2_f;
   if (fabsf(d2 - P.rho2_f) <= P.band_f)
   {
-    const uint2 l = lo[j];
+    const uint2 l = __ldg(reinterpret_cast<const uint2 *>(&aux[j]));
     const double ex = (double) (long long) (join64(rj.x, l.x) - Xi) * 5.421010862427522e-20;
     const double ey = (double) (long long) (join64(rj.y, l.y) - Yi) * 5.421010862427522e-20;
     in = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)) <= P.rho2_d;
   }
-  if (in)
-  {
-    float s, c;
-    phase_sincos(rj.z - ri.z, s, c);  // sin, cos of phi_j - phi_i
-    const float wj = __uint_as_float(rj.w);
-    a.ss += s;
-    a.sc += c;
-    a.ws += wj * s;
-    a.wc += wj * c;
-    a.card += 1;
-  }
+  return in;
+}
+
+__device__ __forceinline__ void accumulate(Acc &a, const uint4 &rj, float wj)
+{
+  const float cj = __uint_as_float(rj.z), sj = __uint_as_float(rj.w);
+  a.sc += cj;
+  a.ss += sj;
+  a.wc = fmaf(wj, cj, a.wc);
+  a.ws = fmaf(wj, sj, a.ws);
+  a.card += 1;
+}
+
+template<bool OMEGA>
+__device__ __forceinline__ void candidate(const FastParams &P, const uint4 &ri, uint64_t Xi, uint64_t Yi,
+                                          const uint4 *__restrict__ rec, const uint4 *__restrict__ aux, int j, Acc &a)
+{
+  const uint4 rj = __ldg(&rec[j]);
+  if (in_range(P, ri, Xi, Yi, rj, aux, j)) accumulate(a, rj, OMEGA ? __uint_as_float(__ldg(&aux[j].w)) : 0.0f);
+}
+
+// Four list entries at a time: the entry loads, then the record loads, then
+// the omega loads of the pairs in range are issued together, so a thread has
+// several gathers in flight instead of a chain of dependent ones.
+template<bool OMEGA>
+__device__ __forceinline__ void candidates4(const FastParams &P, const uint4 &ri, uint64_t Xi, uint64_t Yi,
+                                            const uint4 *__restrict__ rec, const uint4 *__restrict__ aux,
+                                            const int j[4], Acc &a)
+{
+  uint4 r[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) r[u] = __ldg(&rec[j[u]]);
+  bool in[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) in[u] = in_range(P, ri, Xi, Yi, r[u], aux, j[u]);
+  float w[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) w[u] = (OMEGA && in[u]) ? __uint_as_float(__ldg(&aux[j[u]].w)) : 0.0f;
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+    if (in[u]) accumulate(a, r[u], w[u]);
 }
 
 // ---------------------------------------------------------------- conversions
 
-// Upload from reference AoS (original order).  With a valid slot order the
-// particle in slot q is pid[q]; otherwise slots are reset to the identity.
+// A block's contiguous AoS rows move between global (possibly host) memory
+// and shared memory in 16-byte pieces when the array allows it, so that reads
+// and writes over the host link are whole coalesced lines.
+__device__ __forceinline__ void rows_to_shared(const double *__restrict__ g, double *sh, int count)
+{
+  if (((uintptr_t) g & 15) == 0)
+  {
+    const double2 *g2 = reinterpret_cast<const double2 *>(g);
+    double2 *s2 = reinterpret_cast<double2 *>(sh);
+    for (int i = threadIdx.x; i < count / 2; i += blockDim.x) s2[i] = g2[i];
+    if ((count & 1) && threadIdx.x == 0) sh[count - 1] = g[count - 1];
+  } else
+  {
+    for (int i = threadIdx.x; i < count; i += blockDim.x) sh[i] = g[i];
+  }
+}
+
+__device__ __forceinline__ void rows_from_shared(double *__restrict__ g, const double *sh, int count)
+{
+  if (((uintptr_t) g & 15) == 0)
+  {
+    double2 *g2 = reinterpret_cast<double2 *>(g);
+    const double2 *s2 = reinterpret_cast<const double2 *>(sh);
+    for (int i = threadIdx.x; i < count / 2; i += blockDim.x) g2[i] = s2[i];
+    if ((count & 1) && threadIdx.x == 0) g[count - 1] = sh[count - 1];
+  } else
+  {
+    for (int i = threadIdx.x; i < count; i += blockDim.x) g[i] = sh[i];
+  }
+}
+
+// Upload from reference AoS, one thread per original index p (its block's
+// rows read as one coalesced chunk), scattered to the particle's slot inv[p]
+// (identity when no slot order exists yet).
 __global__ void fast_upload_kernel(const double *__restrict__ x, int n, int s, int model, int perm_valid,
                                    FastBuffers B)
 {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= n) return;
+  extern __shared__ double rows[];
+  const int p0 = blockIdx.x * blockDim.x;
+  const int count = min((int) blockDim.x, n - p0) * s;
+  rows_to_shared(x + (long) s * p0, rows, count);
+  __syncthreads();
+  const int p = p0 + threadIdx.x;
+  if (p >= n) return;
   const int par = B.ctrl->parity;
-  const unsigned p = perm_valid ? B.pid[q] : (unsigned) q;
-  if (!perm_valid) B.pid[q] = p;
-  const double *st = x + (long) s * p;
+  unsigned q = (unsigned) p;
+  if (perm_valid)
+  {
+    q = B.inv[p];
+  } else
+  {
+    B.pid[p] = (unsigned) p;
+    B.inv[p] = (unsigned) p;
+  }
+  const double *st = rows + s * threadIdx.x;
   int2 im;
   uint64_t X, Y;
   {
@@ -243,37 +320,46 @@ __global__ void fast_upload_kernel(const double *__restrict__ x, int n, int s, i
   const double fr = (t - ft) * 4294967296.0;
   const uint32_t ph = fr >= 4294967295.0 ? 0xffffffffu : (uint32_t) fr;
   const float w = (float) st[ip + 1];
-  uint4 r = make_uint4((uint32_t) (X >> 32), (uint32_t) (Y >> 32), ph, __float_as_uint(w));
-  uint4 *rec = par ? B.rec1 : B.rec0;
-  uint2 *lo = par ? B.lo1 : B.lo0;
-  rec[q] = r;
-  lo[q] = make_uint2((uint32_t) X, (uint32_t) Y);
+  float sp, cp;
+  phase_sincos(ph, sp, cp);
+  (par ? B.rec1 : B.rec0)[q] = make_uint4((uint32_t) (X >> 32), (uint32_t) (Y >> 32), __float_as_uint(cp),
+                                          __float_as_uint(sp));
+  (par ? B.aux1 : B.aux0)[q] = make_uint4((uint32_t) X, (uint32_t) Y, ph, __float_as_uint(w));
   B.img[q] = im;
   B.turns[q] = (int) ft;
   if (model == 2) B.vel[q] = make_float2((float) st[2], (float) st[3]);
 }
 
+// Download to reference AoS, one thread per original index: gathers the slot
+// inv[p]; the block's rows are written as one coalesced chunk.
 __global__ void fast_download_kernel(double *__restrict__ x, int n, int s, int model, FastBuffers B)
 {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= n) return;
-  const int par = B.ctrl->parity;
-  const uint4 r = (par ? B.rec1 : B.rec0)[q];
-  const uint2 l = (par ? B.lo1 : B.lo0)[q];
-  const unsigned p = B.pid[q];
-  const int2 im = B.img[q];
-  double *st = x + (long) s * p;
-  st[0] = (double) im.x + (double) join64(r.x, l.x) * 5.421010862427522e-20;
-  st[1] = (double) im.y + (double) join64(r.y, l.y) * 5.421010862427522e-20;
-  const int ip = model == 1 ? 2 : 4;
-  st[ip] = 6.283185307179586 * ((double) B.turns[q] + (double) r.z * 2.3283064365386963e-10);
-  st[ip + 1] = (double) __uint_as_float(r.w);
-  if (model == 2)
+  extern __shared__ double rows[];
+  const int p0 = blockIdx.x * blockDim.x;
+  const int count = min((int) blockDim.x, n - p0) * s;
+  const int p = p0 + threadIdx.x;
+  if (p < n)
   {
-    const float2 v = B.vel[q];
-    st[2] = v.x;
-    st[3] = v.y;
+    const int par = B.ctrl->parity;
+    const unsigned q = B.inv[p];
+    const uint4 r = (par ? B.rec1 : B.rec0)[q];
+    const uint4 a = (par ? B.aux1 : B.aux0)[q];
+    const int2 im = B.img[q];
+    double *st = rows + s * threadIdx.x;
+    st[0] = (double) im.x + (double) join64(r.x, a.x) * 5.421010862427522e-20;
+    st[1] = (double) im.y + (double) join64(r.y, a.y) * 5.421010862427522e-20;
+    const int ip = model == 1 ? 2 : 4;
+    st[ip] = 6.283185307179586 * ((double) B.turns[q] + (double) a.z * 2.3283064365386963e-10);
+    st[ip + 1] = (double) __uint_as_float(a.w);
+    if (model == 2)
+    {
+      const float2 v = B.vel[q];
+      st[2] = v.x;
+      st[3] = v.y;
+    }
   }
+  __syncthreads();
+  rows_from_shared(x + (long) s * p0, rows, count);
 }
 
 // ---------------------------------------------------------------- rebuild
@@ -284,25 +370,23 @@ __global__ void fast_cells_kernel(FastParams P, FastBuffers B)
   if (q >= P.n) return;
   const int par = B.ctrl->parity;
   const uint4 r = (par ? B.rec1 : B.rec0)[q];
-  const uint2 l = (par ? B.lo1 : B.lo0)[q];
-  B.cell_of[q] = cell_of_fix(join64(r.x, l.x), join64(r.y, l.y), P.nc);
+  const uint4 a = (par ? B.aux1 : B.aux0)[q];
+  B.cell_of[q] = cell_of_fix(join64(r.x, a.x), join64(r.y, a.y), P.nc);
 }
 
 // New slot q takes the particle of old slot order[q] (cells contiguous,
-// ascending old slot inside a cell).  Writes the other rec/lo buffer.
+// ascending old slot inside a cell).  Writes the other rec/aux buffer.
 __global__ void fast_permute_kernel(FastParams P, FastBuffers B)
 {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= P.n) return;
   const int par = B.ctrl->parity;
   const int src = B.order[q];
-  const uint4 *rin = par ? B.rec1 : B.rec0;
-  uint4 *rout = par ? B.rec0 : B.rec1;
-  const uint2 *lin = par ? B.lo1 : B.lo0;
-  uint2 *lout = par ? B.lo0 : B.lo1;
-  rout[q] = rin[src];
-  lout[q] = lin[src];
-  B.pid_tmp[q] = B.pid[src];
+  (par ? B.rec0 : B.rec1)[q] = (par ? B.rec1 : B.rec0)[src];
+  (par ? B.aux0 : B.aux1)[q] = (par ? B.aux1 : B.aux0)[src];
+  const unsigned p = B.pid[src];
+  B.pid_tmp[q] = p;
+  B.inv[p] = (unsigned) q;
   B.img_tmp[q] = B.img[src];
   B.turns_tmp[q] = B.turns[src];
   if (P.model == 2) B.vel_tmp[q] = B.vel[src];
@@ -330,7 +414,9 @@ __global__ void fast_after_rebuild_kernel(FastControl *ctrl, int permuted)
 // Verlet lists from the 3x3 stencil of the rebuild grid (ParticleSystemFirstOrder.cpp:536-589):
 // pairs with r <= r_max (conservatively widened by the guard band; an entry
 // beyond r_max can never come within rho before the next rebuild).  Entry m of
-// slot q at vl[m * n + q]; a count of -1 marks a list longer than the capacity.
+// slot q at vl[m * n + q] as the 16-bit offset j - q; a count of -1 marks a
+// list longer than the capacity or an offset beyond 16 bits (the step then
+// scans the stencil of the rebuild-time cell instead).
 __global__ void fast_verlet_build_kernel(FastParams P, FastBuffers B)
 {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -341,6 +427,8 @@ __global__ void fast_verlet_build_kernel(FastParams P, FastBuffers B)
   const int c = B.cell_sorted[q];
   const int cx = c % P.nc, cy = c / P.nc;
   int cnt = 0;
+  bool far = false;
+  short *lp = B.vl + q;
   for (int sy = -1; sy <= 1; ++sy)
   {
     const int jy = wrap_cell(cy + sy, P.nc);
@@ -351,50 +439,63 @@ __global__ void fast_verlet_build_kernel(FastParams P, FastBuffers B)
       for (int j = B.cell_off[jc]; j < e; ++j)
       {
         if (j == q) continue;
-        const uint4 rj = rec[j];
+        const uint4 rj = __ldg(&rec[j]);
         const float dx = (float) (int) (rj.x - ri.x) * 2.3283064365386963e-10f;
         const float dy = (float) (int) (rj.y - ri.y) * 2.3283064365386963e-10f;
         if (fmaf(dx, dx, dy * dy) <= P.rmax2_f)
         {
-          if (cnt < P.cap) B.vl[(long) cnt * P.n + q] = j;
+          const int off = j - q;
+          if (off < -32768 || off > 32767) far = true;
+          if (cnt < P.cap)
+          {
+            *lp = (short) off;
+            lp += P.n;
+          }
           ++cnt;
         }
       }
     }
   }
-  if (cnt > P.cap)
-  {
-    atomicMax(&B.ctrl->overflow, cnt);
-    cnt = -1;
-  }
-  B.vl_cnt[q] = cnt;
+  if (cnt > P.cap) atomicMax(&B.ctrl->overflow, cnt);
+  B.vl_cnt[q] = (cnt > P.cap || far) ? -1 : cnt;
 }
 
 // ---------------------------------------------------------------- step
 
-template<int KIND>
-__device__ __forceinline__ void gather_sums(const FastParams &P, const FastBuffers &B, const uint4 *rec, const uint2 *lo,
-                                            int q, const uint4 &ri, uint64_t Xi, uint64_t Yi, Acc &a)
+template<int KIND, bool OMEGA>
+__device__ __forceinline__ void gather_sums(const FastParams &P, const FastBuffers &B, const uint4 *__restrict__ rec,
+                                            const uint4 *__restrict__ aux, int q, int cnt, const uint4 &ri,
+                                            uint64_t Xi, uint64_t Yi, Acc &a)
 {
   if (KIND == KIND_VERLET)
   {
-    const int cnt = B.vl_cnt[q];
     if (cnt >= 0)
     {
-      for (int m = 0; m < cnt; ++m)
+      const short *lp = B.vl + q;
+      const long n = P.n;
+      int m = 0;
+      for (; m + 4 <= cnt; m += 4)
       {
-        const int j = B.vl[(long) m * P.n + q];
-        candidate(P, ri, Xi, Yi, __ldg(&rec[j]), lo, j, a);
+        const int j[4] = {q + (int) __ldg(lp), q + (int) __ldg(lp + n), q + (int) __ldg(lp + 2 * n),
+                          q + (int) __ldg(lp + 3 * n)};
+        lp += 4 * n;
+        candidates4<OMEGA>(P, ri, Xi, Yi, rec, aux, j, a);
+      }
+      for (; m < cnt; ++m)
+      {
+        const int j = q + (int) __ldg(lp);
+        lp += n;
+        candidate<OMEGA>(P, ri, Xi, Yi, rec, aux, j, a);
       }
       return;
     }
-    // list longer than the capacity: the stencil of the rebuild-time cell holds
-    // every particle the list would (displacements since the rebuild < skin / 2)
+    // list unusable: the stencil of the rebuild-time cell holds every particle
+    // the list would (displacements since the rebuild < skin / 2)
   }
   if (KIND == KIND_ALL_PAIRS)
   {
     for (int j = 0; j < P.n; ++j)
-      if (j != q) candidate(P, ri, Xi, Yi, __ldg(&rec[j]), lo, j, a);
+      if (j != q) candidate<OMEGA>(P, ri, Xi, Yi, rec, aux, j, a);
     return;
   }
   const int c = B.cell_sorted[q];
@@ -408,63 +509,77 @@ __device__ __forceinline__ void gather_sums(const FastParams &P, const FastBuffe
       const int jc = jy * P.nc + wrap_cell(cx + sx, P.nc);
       const int e = B.cell_off[jc + 1];
       for (int j = B.cell_off[jc]; j < e; ++j)
-        if (j != q) candidate(P, ri, Xi, Yi, __ldg(&rec[j]), lo, j, a);
+        if (j != q) candidate<OMEGA>(P, ri, Xi, Yi, rec, aux, j, a);
     }
   }
 }
 
 // One SE or SRK step of one particle.  STEPPER: 1 stochastic Euler, 2 strong
-// order 1.5 Taylor.  Per-particle FP32 sums of sin/cos(phi_j - phi_i) and
-// omega_j sin/cos(phi_j - phi_i) give the alignment force and the
-// complementary force of the SRK scheme.
+// order 1.5 Taylor.  Neighbour sums of cos, sin, omega cos, omega sin give the
+// alignment force sum sin(phi_j - phi_i - alpha) and, for SRK, the
+// complementary force sum (omega_j - omega_i) cos(phi_j - phi_i - alpha).
 template<int MODEL, int STEPPER, int KIND>
-__global__ void __launch_bounds__(kTB) fast_step_kernel(FastParams P, FastBuffers B)
+__global__ void __launch_bounds__(kTB, 4) fast_step_kernel(FastParams P, FastBuffers B)
 {
-  __shared__ float smax[kTB / 32];
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   FastControl *ctrl = B.ctrl;
   const int par = ctrl->parity;
   const uint4 *rin = par ? B.rec1 : B.rec0;
-  const uint2 *lin = par ? B.lo1 : B.lo0;
+  const uint4 *ain = par ? B.aux1 : B.aux0;
   uint4 *rout = par ? B.rec0 : B.rec1;
-  uint2 *lout = par ? B.lo0 : B.lo1;
+  uint4 *aout = par ? B.aux0 : B.aux1;
   float d2max = 0.0f;
   int err = 0;
   if (q < P.n)
   {
+    const unsigned p = B.pid[q];
     const uint4 ri = rin[q];
-    const uint2 li = lin[q];
-    const uint64_t Xi = join64(ri.x, li.x), Yi = join64(ri.y, li.y);
-    const float wi = __uint_as_float(ri.w);
+    const uint4 ai = ain[q];
+    const int cnt = KIND == KIND_VERLET ? B.vl_cnt[q] : 0;
+    float2 v = make_float2(0.f, 0.f);
+    if (MODEL == 2) v = B.vel[q];
+    int2 im = B.img[q];
+    int turns = B.turns[q];
+    // the noise does not depend on the neighbours: drawing it first overlaps
+    // its arithmetic with the loads above (exactly the normals the stepper
+    // consumes, reference draw order)
+    constexpr int kNeed = MODEL == 1 ? (STEPPER == 1 ? 1 : 2) : (STEPPER == 1 ? 3 : 6);
+    float z[6];
+    {
+      NoiseKey nk;
+      nk.seed = P.seed;
+      nk.replica = P.replica;
+      nk.step = ctrl->step;
+      const uint4 u = philox_block(nk, p, 0);
+      box_muller_f32(u.x, u.y, z[0], z[1]);
+      if (kNeed > 2) box_muller_f32(u.z, u.w, z[2], z[3]);
+      if (kNeed > 4)
+      {
+        const uint4 u1 = philox_block(nk, p, 1);
+        box_muller_f32(u1.x, u1.y, z[4], z[5]);
+      }
+    }
+    const uint64_t Xi = join64(ri.x, ai.x), Yi = join64(ri.y, ai.y);
+    const float cphi = __uint_as_float(ri.z), sphi = __uint_as_float(ri.w);
+    const float wi = __uint_as_float(ai.w);
     Acc a{0.f, 0.f, 0.f, 0.f, 0};
-    gather_sums<KIND>(P, B, rin, lin, q, ri, Xi, Yi, a);
-    float sphi, cphi;
-    phase_sincos(ri.z, sphi, cphi);
-    // alignment: sum sin(phi_j - phi_i - alpha); complementary: sum (w_j - w_i) cos(phi_j - phi_i - alpha)
+    gather_sums<KIND, STEPPER == 2>(P, B, rin, ain, q, cnt, ri, Xi, Yi, a);
     float f_w = 0.0f, C = 0.0f;  // SE/SRK zero-fill the derivative: an isolated particle keeps 0
     if (a.card > 0)
     {
       const float inv = 1.0f / (float) a.card;
-      const float F = P.ca * a.ss - P.sa * a.sc;
-      f_w = -P.xi_phi * wi + P.sigma * F * inv;
+      const float S = cphi * a.ss - sphi * a.sc;  // sum sin(phi_j - phi_i)
+      const float K = cphi * a.sc + sphi * a.ss;  // sum cos(phi_j - phi_i)
+      f_w = -P.xi_phi * wi + P.sigma * (P.ca * S - P.sa * K) * inv;
       if (STEPPER == 2)
       {
-        const float G = P.ca * (a.wc - wi * a.sc) + P.sa * (a.ws - wi * a.ss);
-        C = P.sigma * inv * G;
+        const float WS = cphi * a.ws - sphi * a.wc;  // sum omega_j sin(phi_j - phi_i)
+        const float WK = cphi * a.wc + sphi * a.ws;  // sum omega_j cos(phi_j - phi_i)
+        C = P.sigma * inv * ((P.ca * WK + P.sa * WS) - wi * (P.ca * K + P.sa * S));
       }
     }
-    const unsigned p = B.pid[q];
-    NoiseKey nk;
-    nk.seed = P.seed;
-    nk.replica = P.replica;
-    nk.step = ctrl->step;
-    float z[8];
-    normals4_f32(nk, p, 0, z);
-    if (STEPPER == 2 && MODEL == 2) normals4_f32(nk, p, 1, z + 4);
     const float dt = P.dt;
     float ddx, ddy, dphi, dw;
-    int2 im = B.img[q];
-    int turns = B.turns[q];
     const int2 im0 = im;
     const int turns0 = turns;
     if (MODEL == 1)
@@ -489,7 +604,6 @@ __global__ void __launch_bounds__(kTB) fast_step_kernel(FastParams P, FastBuffer
       }
     } else
     {
-      const float2 v = B.vel[q];
       const float fvx = -P.xi_r * v.x + P.v0 * cphi, fvy = -P.xi_r * v.y + P.v0 * sphi;
       float dvx, dvy;
       if (STEPPER == 1)
@@ -518,28 +632,25 @@ __global__ void __launch_bounds__(kTB) fast_step_kernel(FastParams P, FastBuffer
     }
     const uint64_t Xn = advance(Xi, fix64_of(ddx, err), im.x);
     const uint64_t Yn = advance(Yi, fix64_of(ddy, err), im.y);
-    const uint32_t Pn = advance_phase(ri.z, dphi, turns, err);
-    rout[q] = make_uint4((uint32_t) (Xn >> 32), (uint32_t) (Yn >> 32), Pn, __float_as_uint(wi + dw));
-    lout[q] = make_uint2((uint32_t) Xn, (uint32_t) Yn);
+    const uint32_t Pn = advance_phase(ai.z, dphi, turns, err);
+    float sn, cn;
+    phase_sincos(Pn, sn, cn);
+    rout[q] = make_uint4((uint32_t) (Xn >> 32), (uint32_t) (Yn >> 32), __float_as_uint(cn), __float_as_uint(sn));
+    aout[q] = make_uint4((uint32_t) Xn, (uint32_t) Yn, Pn, __float_as_uint(wi + dw));
     if (im.x != im0.x || im.y != im0.y) B.img[q] = im;
     if (turns != turns0) B.turns[q] = turns;
     d2max = fmaf(ddx, ddx, ddy * ddy);
   }
-  // block max of |dr|^2 for the Verlet trigger
+  // warp max of |dr|^2 for the Verlet trigger; a warp issues its atomic only
+  // when it can raise the maximum already stored (no block barrier)
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) d2max = fmaxf(d2max, __shfl_xor_sync(0xffffffffu, d2max, off));
-  if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = d2max;
-  err = __syncthreads_or(err);
-  if (threadIdx.x < 32)
+  err = __any_sync(0xffffffffu, err);
+  if ((threadIdx.x & 31) == 0)
   {
-    float m = threadIdx.x < kTB / 32 ? smax[threadIdx.x] : 0.0f;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
-    if (threadIdx.x == 0)
-    {
-      atomicMax(&ctrl->max2_bits, __float_as_uint(m));
-      if (err) atomicOr(&ctrl->error, 1);
-    }
+    const unsigned bits = __float_as_uint(d2max);
+    if (bits > *(volatile unsigned *) &ctrl->max2_bits) atomicMax(&ctrl->max2_bits, bits);
+    if (err) atomicOr(&ctrl->error, 1);
   }
 }
 
@@ -603,12 +714,13 @@ static FastBuffers buffers(spss_ctx *ctx)
   FastBuffers B;
   B.rec0 = f->rec[0].ptr;
   B.rec1 = f->rec[1].ptr;
-  B.lo0 = f->lo[0].ptr;
-  B.lo1 = f->lo[1].ptr;
+  B.aux0 = f->aux[0].ptr;
+  B.aux1 = f->aux[1].ptr;
   B.vel = f->vel.ptr;
   B.vel_tmp = f->vel_tmp.ptr;
   B.pid = f->pid.ptr;
   B.pid_tmp = f->pid_tmp.ptr;
+  B.inv = f->inv.ptr;
   B.img = f->img.ptr;
   B.img_tmp = f->img_tmp.ptr;
   B.turns = f->turns.ptr;
@@ -619,7 +731,6 @@ static FastBuffers buffers(spss_ctx *ctx)
   B.order = f->binner.members.ptr;
   B.vl = f->vl.ptr;
   B.vl_cnt = f->vl_cnt.ptr;
-  B.caf = f->caf.ptr;
   B.ctrl = f->ctrl;
   return B;
 }
@@ -698,19 +809,19 @@ int fast_create(spss_ctx *ctx)
   for (int b = 0; b < 2; ++b)
   {
     SPSS_TRY(f->rec[b].reserve(n));
-    SPSS_TRY(f->lo[b].reserve(n));
+    SPSS_TRY(f->aux[b].reserve(n));
   }
   SPSS_TRY(f->vel.reserve(n));
   SPSS_TRY(f->vel_tmp.reserve(n));
   SPSS_TRY(f->pid.reserve(n));
   SPSS_TRY(f->pid_tmp.reserve(n));
+  SPSS_TRY(f->inv.reserve(n));
   SPSS_TRY(f->img.reserve(n));
   SPSS_TRY(f->img_tmp.reserve(n));
   SPSS_TRY(f->turns.reserve(n));
   SPSS_TRY(f->turns_tmp.reserve(n));
   SPSS_TRY(f->cell_of.reserve(n));
   SPSS_TRY(f->cell_sorted.reserve(n));
-  SPSS_TRY(f->caf.reserve(n));
   SPSS_TRY(f->vl_cnt.reserve(n));
   if (f->kind == KIND_VERLET)
   {
@@ -742,12 +853,13 @@ void fast_destroy(spss_ctx *ctx)
   for (int b = 0; b < 2; ++b)
   {
     f->rec[b].release();
-    f->lo[b].release();
+    f->aux[b].release();
   }
   f->vel.release();
   f->vel_tmp.release();
   f->pid.release();
   f->pid_tmp.release();
+  f->inv.release();
   f->img.release();
   f->img_tmp.release();
   f->turns.release();
@@ -756,7 +868,6 @@ void fast_destroy(spss_ctx *ctx)
   f->cell_sorted.release();
   f->vl.release();
   f->vl_cnt.release();
-  f->caf.release();
   f->binner.release();
   if (f->ctrl) cudaFree(f->ctrl);
   if (f->h_ctrl) cudaFreeHost(f->h_ctrl);
@@ -857,8 +968,8 @@ static int push_host_control(spss_ctx *ctx)
 int fast_set_state(spss_ctx *ctx, const double *d_aos)
 {
   FastPath *f = ctx->fast;
-  fast_upload_kernel<<<blocks_for(ctx->p.n, kTB), kTB, 0, ctx->stream>>>(d_aos, ctx->p.n, ctx->s, ctx->p.model,
-                                                                        f->perm_valid ? 1 : 0, buffers(ctx));
+  fast_upload_kernel<<<blocks_for(ctx->p.n, kTB), kTB, sizeof(double) * kTB * ctx->s, ctx->stream>>>(
+      d_aos, ctx->p.n, ctx->s, ctx->p.model, f->perm_valid ? 1 : 0, buffers(ctx));
   ++ctx->launches;
   SPSS_TRY(check_launch("fast_upload_kernel"));
   f->perm_valid = true;
@@ -868,8 +979,8 @@ int fast_set_state(spss_ctx *ctx, const double *d_aos)
 
 int fast_get_state(spss_ctx *ctx, double *d_aos)
 {
-  fast_download_kernel<<<blocks_for(ctx->p.n, kTB), kTB, 0, ctx->stream>>>(d_aos, ctx->p.n, ctx->s, ctx->p.model,
-                                                                          buffers(ctx));
+  fast_download_kernel<<<blocks_for(ctx->p.n, kTB), kTB, sizeof(double) * kTB * ctx->s, ctx->stream>>>(
+      d_aos, ctx->p.n, ctx->s, ctx->p.model, buffers(ctx));
   ++ctx->launches;
   return check_launch("fast_download_kernel");
 }

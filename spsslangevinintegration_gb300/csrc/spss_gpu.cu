@@ -454,21 +454,34 @@ int spss_step_host(spss_ctx *ctx, int stepper, double *state, long len, double t
   {
     if (ctx->registered_host) cudaHostUnregister(ctx->registered_host);
     ctx->registered_host = nullptr;
-    if (cudaHostRegister(state, bytes, cudaHostRegisterDefault) == cudaSuccess)
+    ctx->registered_device = nullptr;
+    if (cudaHostRegister(state, bytes, cudaHostRegisterMapped) == cudaSuccess)
     {
       ctx->registered_host = state;
       ctx->registered_bytes = bytes;
+      void *dp = nullptr;
+      if (cudaHostGetDevicePointer(&dp, state, 0) == cudaSuccess) ctx->registered_device = (double *) dp;
+      cudaGetLastError();
     } else
     {
       cudaGetLastError();  // pageable copies still work
     }
   }
-  SPSS_TRY(ctx->scratch_a.reserve(len));
-  SPSS_CUDA_TRY(cudaMemcpyAsync(ctx->scratch_a.ptr, state, bytes, cudaMemcpyHostToDevice, ctx->stream));
-  SPSS_TRY(is_f64(ctx) ? f64_set_state(ctx, ctx->scratch_a.ptr) : fast_set_state(ctx, ctx->scratch_a.ptr));
+  // Registered and mapped: the upload kernel reads the caller's array over the
+  // host link and the download kernel writes it back, each in one pass that
+  // also converts the layout.  Otherwise stage through device memory.
+  double *io = ctx->registered_device;
+  if (!io)
+  {
+    SPSS_TRY(ctx->scratch_a.reserve(len));
+    SPSS_CUDA_TRY(cudaMemcpyAsync(ctx->scratch_a.ptr, state, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  const double *in = io ? io : ctx->scratch_a.ptr;
+  double *out = io ? io : ctx->scratch_a.ptr;
+  SPSS_TRY(is_f64(ctx) ? f64_set_state(ctx, in) : fast_set_state(ctx, in));
   SPSS_TRY(is_f64(ctx) ? f64_step(ctx, stepper, t, dt) : fast_step(ctx, stepper, t, dt));
-  SPSS_TRY(is_f64(ctx) ? f64_get_state(ctx, ctx->scratch_a.ptr) : fast_get_state(ctx, ctx->scratch_a.ptr));
-  SPSS_CUDA_TRY(cudaMemcpyAsync(state, ctx->scratch_a.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  SPSS_TRY(is_f64(ctx) ? f64_get_state(ctx, out) : fast_get_state(ctx, out));
+  if (!io) SPSS_CUDA_TRY(cudaMemcpyAsync(state, ctx->scratch_a.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream));
   SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return SPSS_OK;
 }
