@@ -84,6 +84,8 @@ struct FastBuffers
   const int *order;
   short *vl;
   int *vl_cnt;
+  int *tile_maxcnt;  // longest list of each tile (rows to stage)
+  void *tiles;       // TileLayout of every tile, written at rebuild
   FastControl *ctrl;
 };
 
@@ -101,8 +103,9 @@ struct FastPath
   DeviceArray<float2> vel, vel_tmp;
   DeviceArray<unsigned> pid, pid_tmp, inv;
   DeviceArray<int2> img, img_tmp;
-  DeviceArray<int> turns, turns_tmp, cell_of, cell_sorted, vl_cnt;
+  DeviceArray<int> turns, turns_tmp, cell_of, cell_sorted, vl_cnt, tile_maxcnt;
   DeviceArray<short> vl;
+  DeviceArray<unsigned char> tiles;
   Binner binner;
   FastControl *ctrl = nullptr;    // device
   FastControl *h_ctrl = nullptr;  // pinned mirror
@@ -139,19 +142,19 @@ __device__ __forceinline__ long long fix64_of(float f, int &err)
   return (b >> 31) ? -v : v;
 }
 
-// X += dX on the periodic unit box; the image counter follows the carry.
-__device__ __forceinline__ uint64_t advance(uint64_t X, long long dX, int &img)
+// X += dX on the periodic unit box; `carry` receives the box crossing (-1, 0, 1).
+__device__ __forceinline__ uint64_t advance(uint64_t X, long long dX, int &carry)
 {
   const uint64_t Y = X + (uint64_t) dX;
-  if (dX > 0 && Y < X) ++img;
-  if (dX < 0 && Y > X) --img;
+  carry = (dX > 0 && Y < X) ? 1 : ((dX < 0 && Y > X) ? -1 : 0);
   return Y;
 }
 
-__device__ __forceinline__ uint32_t advance_phase(uint32_t P, float dphi, int &turns, int &err)
+__device__ __forceinline__ uint32_t advance_phase(uint32_t P, float dphi, int &carry, int &err)
 {
   // 2^32 / (2 pi)
   const float q = dphi * 683565275.5764316f;
+  carry = 0;
   if (!(fabsf(q) < 2.1e9f))
   {
     err = 1;
@@ -159,8 +162,7 @@ __device__ __forceinline__ uint32_t advance_phase(uint32_t P, float dphi, int &t
   }
   const int d = __float2int_rn(q);
   const uint32_t R = P + (uint32_t) d;
-  if (d > 0 && R < P) ++turns;
-  if (d < 0 && R > P) --turns;
+  carry = (d > 0 && R < P) ? 1 : ((d < 0 && R > P) ? -1 : 0);
   return R;
 }
 
@@ -194,8 +196,8 @@ struct Acc
 __device__ __forceinline__ bool in_range(const FastParams &P, const uint4 &ri, uint64_t Xi, uint64_t Yi,
                                          const uint4 &rj, const uint4 *__restrict__ aux, int j)
 {
-  const float dx = (float) (int) (rj.x - ri.x) * 2.3283064365386963e-10f;
-  const float dy = (float) (int) (rj.y - ri.y) * 2.3283064365386963e-10f;
+  const float dx = (float) (int) (rj.x - ri.x);
+  const float dy = (float) (int) (rj.y - ri.y);
   const float d2 = fmaf(dx, dx, dy * dy);
   bool in = d2 <= P.rho2_f;
   if (fabsf(d2 - P.rho2_f) <= P.band_f)
@@ -411,12 +413,158 @@ __global__ void fast_after_rebuild_kernel(FastControl *ctrl, int permuted)
   ctrl->rebuilds += 1;
 }
 
+// ---------------------------------------------------------------- tiles
+//
+// A tile is a run of kTileCells cells of one row of the rebuild grid; one CTA
+// steps the particles of a tile.  Slots are sorted by cell, so the tile's
+// particles are one slot range and the records of its 3 x (kTileCells + 2)
+// neighbour cells are at most six slot segments (three rows, each split in
+// two where the periodic x-wrap crosses the row end).  The CTA stages those
+// segments into shared memory with TMA bulk copies; the Verlet list of a
+// particle in a staged tile stores shared-memory indices directly.
+
+constexpr int kTileCells = 32;    // cells per tile
+constexpr int kTileCap = 512;     // staged neighbour records per CTA (2 x 8 KiB)
+constexpr int kTileThreads = 128;
+constexpr long long kWaitCycles = 1ll << 31;  // about one second at the SM clock
+
+struct TileLayout
+{
+  int p_begin, p_end;  // slots of the tile's own particles
+  int nseg, total;     // staged segments (ascending slot order) and records
+  int start[6], len[6], base[6];
+  int staged;          // the neighbourhood fits kTileCap records
+};
+
+__host__ __device__ __forceinline__ int tiles_per_row(int nc)
+{
+  return (nc + kTileCells - 1) / kTileCells;
+}
+
+// Deterministic layout of tile t (the list build and the step compute the same).
+__device__ void tile_layout(int t, int nc, const int *__restrict__ off, TileLayout &L)
+{
+  const int nbx = tiles_per_row(nc);
+  const int cy = t / nbx, bx = t - cy * nbx;
+  const int cx_lo = bx * kTileCells, cx_hi = min(nc, cx_lo + kTileCells);
+  L.p_begin = off[cy * nc + cx_lo];
+  L.p_end = off[cy * nc + cx_hi];
+  L.nseg = 0;
+  L.total = 0;
+  L.staged = 0;
+  if (nc < 3) return;  // rows would repeat in the stencil
+  int st[6], en[6], ns = 0;
+  const bool whole_row = (cx_hi - cx_lo + 2) >= nc;
+  for (int dy = -1; dy <= 1; ++dy)
+  {
+    const int row = wrap_cell(cy + dy, nc) * nc;
+    if (whole_row)
+    {
+      st[ns] = off[row];
+      en[ns++] = off[row + nc];
+    } else if (cx_lo == 0)
+    {
+      st[ns] = off[row];  // cells 0 .. cx_hi
+      en[ns++] = off[row + cx_hi + 1];
+      st[ns] = off[row + nc - 1];  // left neighbour wraps to the last cell
+      en[ns++] = off[row + nc];
+    } else if (cx_hi == nc)
+    {
+      st[ns] = off[row];  // right neighbour wraps to the first cell
+      en[ns++] = off[row + 1];
+      st[ns] = off[row + cx_lo - 1];
+      en[ns++] = off[row + nc];
+    } else
+    {
+      st[ns] = off[row + cx_lo - 1];
+      en[ns++] = off[row + cx_hi + 1];
+    }
+  }
+  for (int a = 1; a < ns; ++a)
+  {
+    const int s0 = st[a], e0 = en[a];
+    int b = a - 1;
+    while (b >= 0 && st[b] > s0)
+    {
+      st[b + 1] = st[b];
+      en[b + 1] = en[b];
+      --b;
+    }
+    st[b + 1] = s0;
+    en[b + 1] = e0;
+  }
+  for (int a = 0; a < ns; ++a)
+  {
+    if (en[a] <= st[a]) continue;
+    L.start[L.nseg] = st[a];
+    L.len[L.nseg] = en[a] - st[a];
+    L.base[L.nseg] = L.total;
+    L.total += en[a] - st[a];
+    ++L.nseg;
+  }
+  L.staged = L.total <= kTileCap;
+}
+
+__device__ __forceinline__ int tile_of_cell(int c, int nc)
+{
+  const int cy = c / nc;
+  return cy * tiles_per_row(nc) + (c - cy * nc) / kTileCells;
+}
+
+// Layout of every tile of the rebuild grid, once per rebuild.
+__global__ void fast_tile_layout_kernel(FastParams P, FastBuffers B)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= P.nc * tiles_per_row(P.nc)) return;
+  TileLayout L;
+  tile_layout(t, P.nc, B.cell_off, L);
+  reinterpret_cast<TileLayout *>(B.tiles)[t] = L;
+}
+
+// Tile-major Verlet lists: tile t keeps rows m = 0 .. cap-1 of its particles
+// contiguously, row stride round_up8(particles of the tile) entries, starting
+// at cap * round_up8(p_begin + 16 t) (16-byte aligned, never overlapping the
+// next tile); a tile's list rows are thus one block a bulk copy can stage.
+__device__ __forceinline__ long tile_list_base(int cap, int t, int p_begin)
+{
+  return (long) cap * (long) ((p_begin + 16 * t + 7) & ~7);
+}
+
+__device__ __forceinline__ int tile_list_stride(int p_begin, int p_end)
+{
+  return (p_end - p_begin + 7) & ~7;
+}
+
+constexpr int kListCap = 4096;  // staged list entries per CTA (8 KiB)
+
+// Shared-memory index of slot j inside the staged segments (-1: not staged).
+__device__ __forceinline__ int staged_index(const TileLayout &L, int j)
+{
+  for (int k = 0; k < L.nseg; ++k)
+    if (j >= L.start[k] && j < L.start[k] + L.len[k]) return L.base[k] + (j - L.start[k]);
+  return -1;
+}
+
+// Slot of a staged index (rare path: the guard band needs the slot's low words).
+__device__ __forceinline__ int staged_slot(const TileLayout &L, int idx)
+{
+  for (int k = 0; k < L.nseg; ++k)
+    if (idx >= L.base[k] && idx < L.base[k] + L.len[k]) return L.start[k] + (idx - L.base[k]);
+  return 0;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+  return (uint32_t) __cvta_generic_to_shared(p);
+}
+
 // Verlet lists from the 3x3 stencil of the rebuild grid (ParticleSystemFirstOrder.cpp:536-589):
 // pairs with r <= r_max (conservatively widened by the guard band; an entry
 // beyond r_max can never come within rho before the next rebuild).  Entry m of
-// slot q at vl[m * n + q] as the 16-bit offset j - q; a count of -1 marks a
-// list longer than the capacity or an offset beyond 16 bits (the step then
-// scans the stencil of the rebuild-time cell instead).
+// slot q at vl[m * n + q] (16 bits): the neighbour's shared-memory index when
+// q's tile is staged, else the offset j - q.  A count of -1 marks a list
+// longer than the capacity or an offset beyond 16 bits; the step then scans
+// the stencil of the rebuild-time cell instead.
 __global__ void fast_verlet_build_kernel(FastParams P, FastBuffers B)
 {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -426,9 +574,12 @@ __global__ void fast_verlet_build_kernel(FastParams P, FastBuffers B)
   const uint4 ri = rec[q];
   const int c = B.cell_sorted[q];
   const int cx = c % P.nc, cy = c / P.nc;
+  const int t = tile_of_cell(c, P.nc);
+  const TileLayout L = reinterpret_cast<const TileLayout *>(B.tiles)[t];
   int cnt = 0;
   bool far = false;
-  short *lp = B.vl + q;
+  const int stride = tile_list_stride(L.p_begin, L.p_end);
+  short *lp = B.vl + tile_list_base(P.cap, t, L.p_begin) + (q - L.p_begin);
   for (int sy = -1; sy <= 1; ++sy)
   {
     const int jy = wrap_cell(cy + sy, P.nc);
@@ -440,16 +591,24 @@ __global__ void fast_verlet_build_kernel(FastParams P, FastBuffers B)
       {
         if (j == q) continue;
         const uint4 rj = __ldg(&rec[j]);
-        const float dx = (float) (int) (rj.x - ri.x) * 2.3283064365386963e-10f;
-        const float dy = (float) (int) (rj.y - ri.y) * 2.3283064365386963e-10f;
+        const float dx = (float) (int) (rj.x - ri.x);
+        const float dy = (float) (int) (rj.y - ri.y);
         if (fmaf(dx, dx, dy * dy) <= P.rmax2_f)
         {
-          const int off = j - q;
-          if (off < -32768 || off > 32767) far = true;
+          int entry;
+          if (L.staged)
+          {
+            entry = staged_index(L, j);
+            if (entry < 0) far = true;
+          } else
+          {
+            entry = j - q;
+            if (entry < -32768 || entry > 32767) far = true;
+          }
           if (cnt < P.cap)
           {
-            *lp = (short) off;
-            lp += P.n;
+            *lp = (short) entry;
+            lp += stride;
           }
           ++cnt;
         }
@@ -457,33 +616,34 @@ __global__ void fast_verlet_build_kernel(FastParams P, FastBuffers B)
     }
   }
   if (cnt > P.cap) atomicMax(&B.ctrl->overflow, cnt);
+  atomicMax(&B.tile_maxcnt[t], min(cnt, P.cap));
   B.vl_cnt[q] = (cnt > P.cap || far) ? -1 : cnt;
 }
 
 // ---------------------------------------------------------------- step
 
+// Neighbour sums of slot q from global memory (per-slot kernel, and tiles
+// that do not fit shared memory): the Verlet list holds slot offsets.
 template<int KIND, bool OMEGA>
 __device__ __forceinline__ void gather_sums(const FastParams &P, const FastBuffers &B, const uint4 *__restrict__ rec,
-                                            const uint4 *__restrict__ aux, int q, int cnt, const uint4 &ri,
-                                            uint64_t Xi, uint64_t Yi, Acc &a)
+                                            const uint4 *__restrict__ aux, int q, int cnt, const short *lp, int stride,
+                                            const uint4 &ri, uint64_t Xi, uint64_t Yi, Acc &a)
 {
   if (KIND == KIND_VERLET)
   {
     if (cnt >= 0)
     {
-      const short *lp = B.vl + q;
-      const long n = P.n;
+      const long n = stride;
       int m = 0;
       for (; m + 4 <= cnt; m += 4)
       {
-        const int j[4] = {q + (int) __ldg(lp), q + (int) __ldg(lp + n), q + (int) __ldg(lp + 2 * n),
-                          q + (int) __ldg(lp + 3 * n)};
+        const int j[4] = {q + (int) lp[0], q + (int) lp[n], q + (int) lp[2 * n], q + (int) lp[3 * n]};
         lp += 4 * n;
         candidates4<OMEGA>(P, ri, Xi, Yi, rec, aux, j, a);
       }
       for (; m < cnt; ++m)
       {
-        const int j = q + (int) __ldg(lp);
+        const int j = q + (int) lp[0];
         lp += n;
         candidate<OMEGA>(P, ri, Xi, Yi, rec, aux, j, a);
       }
@@ -514,10 +674,211 @@ __device__ __forceinline__ void gather_sums(const FastParams &P, const FastBuffe
   }
 }
 
-// One SE or SRK step of one particle.  STEPPER: 1 stochastic Euler, 2 strong
-// order 1.5 Taylor.  Neighbour sums of cos, sin, omega cos, omega sin give the
-// alignment force sum sin(phi_j - phi_i - alpha) and, for SRK, the
-// complementary force sum (omega_j - omega_i) cos(phi_j - phi_i - alpha).
+// One staged candidate: the record comes from shared memory; the guard band
+// (rare) still reads the slot's low position words from global memory.
+template<bool OMEGA>
+__device__ __forceinline__ void candidate_staged(const FastParams &P, const uint4 &ri, uint64_t Xi, uint64_t Yi,
+                                                 const uint4 *srec, const uint4 *saux, int idx, Acc &a)
+{
+  const uint4 rj = srec[idx];
+  const float dx = (float) (int) (rj.x - ri.x);
+  const float dy = (float) (int) (rj.y - ri.y);
+  const float d2 = fmaf(dx, dx, dy * dy);
+  bool in = d2 <= P.rho2_f;
+  if (fabsf(d2 - P.rho2_f) <= P.band_f)
+  {
+    const uint4 l = saux[idx];
+    const double ex = (double) (long long) (join64(rj.x, l.x) - Xi) * 5.421010862427522e-20;
+    const double ey = (double) (long long) (join64(rj.y, l.y) - Yi) * 5.421010862427522e-20;
+    in = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)) <= P.rho2_d;
+  }
+  if (in) accumulate(a, rj, OMEGA ? __uint_as_float(saux[idx].w) : 0.0f);
+}
+
+// Neighbour sums of slot q from the tile's staged records.
+template<int KIND, bool OMEGA>
+__device__ __forceinline__ void gather_sums_staged(const FastParams &P, const FastBuffers &B, const uint4 *srec,
+                                                   const uint4 *saux, const TileLayout &L,
+                                                   const uint4 *__restrict__ rec, const uint4 *__restrict__ aux, int q,
+                                                   int cnt, const short *lp, int stride, const uint4 &ri, uint64_t Xi,
+                                                   uint64_t Yi, Acc &a)
+{
+  if (KIND == KIND_VERLET && cnt >= 0)
+  {
+    const long n = stride;
+    int m = 0;
+    for (; m + 4 <= cnt; m += 4)
+    {
+      const int i0 = lp[0], i1 = lp[n], i2 = lp[2 * n], i3 = lp[3 * n];
+      lp += 4 * n;
+      candidate_staged<OMEGA>(P, ri, Xi, Yi, srec, saux, i0, a);
+      candidate_staged<OMEGA>(P, ri, Xi, Yi, srec, saux, i1, a);
+      candidate_staged<OMEGA>(P, ri, Xi, Yi, srec, saux, i2, a);
+      candidate_staged<OMEGA>(P, ri, Xi, Yi, srec, saux, i3, a);
+    }
+    for (; m < cnt; ++m)
+    {
+      candidate_staged<OMEGA>(P, ri, Xi, Yi, srec, saux, lp[0], a);
+      lp += n;
+    }
+    return;
+  }
+  // cell list, or a Verlet list that did not fit: scan the stencil of the
+  // (rebuild-time) cell; each stencil cell is one contiguous staged range
+  const int c = B.cell_sorted[q];
+  const int cx = c % P.nc, cy = c / P.nc;
+  for (int sy = -1; sy <= 1; ++sy)
+  {
+    const int jy = wrap_cell(cy + sy, P.nc);
+    for (int sx = -1; sx <= 1; ++sx)
+    {
+      const int jc = jy * P.nc + wrap_cell(cx + sx, P.nc);
+      const int b = B.cell_off[jc], e = B.cell_off[jc + 1];
+      if (e <= b) continue;
+      const int i0 = staged_index(L, b);
+      if (i0 < 0 || i0 + (e - b) > L.total)
+      {
+        // not inside the staged segments (cannot happen for a cell of this tile's stencil)
+        for (int j = b; j < e; ++j)
+          if (j != q) candidate<OMEGA>(P, ri, Xi, Yi, rec, aux, j, a);
+        continue;
+      }
+      const int self = q - b;
+      for (int u = 0; u < e - b; ++u)
+        if (u != self) candidate_staged<OMEGA>(P, ri, Xi, Yi, srec, saux, i0 + u, a);
+    }
+  }
+}
+
+// Exactly the normals the stepper consumes, in the reference's draw order.
+template<int MODEL, int STEPPER>
+__device__ __forceinline__ void draw_noise(const FastParams &P, unsigned long long step, unsigned p, float z[6])
+{
+  constexpr int kNeed = MODEL == 1 ? (STEPPER == 1 ? 1 : 2) : (STEPPER == 1 ? 3 : 6);
+  NoiseKey nk;
+  nk.seed = P.seed;
+  nk.replica = P.replica;
+  nk.step = step;
+  const uint4 u = philox_block(nk, p, 0);
+  box_muller_f32(u.x, u.y, z[0], z[1]);
+  if (kNeed > 2) box_muller_f32(u.z, u.w, z[2], z[3]);
+  if (kNeed > 4)
+  {
+    const uint4 u1 = philox_block(nk, p, 1);
+    box_muller_f32(u1.x, u1.y, z[4], z[5]);
+  }
+}
+
+// Derivative from the neighbour sums, SE or SRK update in fixed point, new
+// record.  Returns |dr|^2 of the step.
+template<int MODEL, int STEPPER>
+__device__ __forceinline__ float update_particle(const FastParams &P, const FastBuffers &B, int q, const uint4 &ri,
+                                                 const uint4 &ai, float2 v, const Acc &a, const float z[6],
+                                                 uint4 *rout, uint4 *aout, int &err)
+{
+  const uint64_t Xi = join64(ri.x, ai.x), Yi = join64(ri.y, ai.y);
+  const float cphi = __uint_as_float(ri.z), sphi = __uint_as_float(ri.w);
+  const float wi = __uint_as_float(ai.w);
+  // sum sin(phi_j - phi_i - alpha) and sum (omega_j - omega_i) cos(phi_j - phi_i - alpha)
+  float f_w = 0.0f, C = 0.0f;  // SE/SRK zero-fill the derivative: an isolated particle keeps 0
+  if (a.card > 0)
+  {
+    const float inv = 1.0f / (float) a.card;
+    const float S = cphi * a.ss - sphi * a.sc;  // sum sin(phi_j - phi_i)
+    const float K = cphi * a.sc + sphi * a.ss;  // sum cos(phi_j - phi_i)
+    f_w = -P.xi_phi * wi + P.sigma * (P.ca * S - P.sa * K) * inv;
+    if (STEPPER == 2)
+    {
+      const float WS = cphi * a.ws - sphi * a.wc;  // sum omega_j sin(phi_j - phi_i)
+      const float WK = cphi * a.wc + sphi * a.ws;  // sum omega_j cos(phi_j - phi_i)
+      C = P.sigma * inv * ((P.ca * WK + P.sa * WS) - wi * (P.ca * K + P.sa * S));
+    }
+  }
+  const float dt = P.dt;
+  float ddx, ddy, dphi, dw;
+  if (MODEL == 1)
+  {
+    const float fx = P.v0 * cphi, fy = P.v0 * sphi, fp = wi;
+    if (STEPPER == 1)
+    {
+      // StochasticEulerStepperPtr.hpp:58-66
+      ddx = fx * dt;
+      ddy = fy * dt;
+      dphi = fp * dt;
+      dw = f_w * dt + P.b_phi * (P.sqdt * z[0]);
+    } else
+    {
+      // StochasticRungeKuttaStepperPtr.hpp:54-70
+      const float dW = z[0] * P.sqdt;
+      const float dZ = P.half_dt15 * (z[0] + P.inv_sqrt3 * z[1]);
+      ddx = fx * dt - fp * fy * P.half_dt2;
+      ddy = fy * dt + fp * fx * P.half_dt2;
+      dphi = fp * dt + f_w * P.half_dt2 + P.b_phi * dZ;
+      dw = f_w * dt + (C - P.xi * f_w) * P.half_dt2 + P.b_phi * (dW - P.xi * dZ);
+    }
+  } else
+  {
+    const float fvx = -P.xi_r * v.x + P.v0 * cphi, fvy = -P.xi_r * v.y + P.v0 * sphi;
+    float dvx, dvy;
+    if (STEPPER == 1)
+    {
+      // StochasticEulerStepper.hpp:44-50 with AddNoise (ParticleSystemSecondOrder.cpp:447-449)
+      ddx = dt * v.x;
+      ddy = dt * v.y;
+      dvx = dt * fvx + P.sqdt * (P.b_r * z[0]);
+      dvy = dt * fvy + P.sqdt * (P.b_r * z[1]);
+      dphi = dt * wi;
+      dw = dt * f_w + P.sqdt * (P.b_phi * z[2]);
+    } else
+    {
+      // second-order strong order 1.5 Taylor scheme (no reference code)
+      const float dWx = z[0] * P.sqdt, dZx = P.half_dt15 * (z[0] + P.inv_sqrt3 * z[1]);
+      const float dWy = z[2] * P.sqdt, dZy = P.half_dt15 * (z[2] + P.inv_sqrt3 * z[3]);
+      const float dWw = z[4] * P.sqdt, dZw = P.half_dt15 * (z[4] + P.inv_sqrt3 * z[5]);
+      ddx = v.x * dt + fvx * P.half_dt2 + P.b_r * dZx;
+      ddy = v.y * dt + fvy * P.half_dt2 + P.b_r * dZy;
+      dvx = fvx * dt + (-P.xi_r * fvx - P.v0 * sphi * wi) * P.half_dt2 + P.b_r * (dWx - P.xi_r * dZx);
+      dvy = fvy * dt + (-P.xi_r * fvy + P.v0 * cphi * wi) * P.half_dt2 + P.b_r * (dWy - P.xi_r * dZy);
+      dphi = wi * dt + f_w * P.half_dt2 + P.b_phi * dZw;
+      dw = f_w * dt + (C - P.xi_phi * f_w) * P.half_dt2 + P.b_phi * (dWw - P.xi_phi * dZw);
+    }
+    B.vel[q] = make_float2(v.x + dvx, v.y + dvy);
+  }
+  int cx, cy, ct;
+  const uint64_t Xn = advance(Xi, fix64_of(ddx, err), cx);
+  const uint64_t Yn = advance(Yi, fix64_of(ddy, err), cy);
+  const uint32_t Pn = advance_phase(ai.z, dphi, ct, err);
+  float sn, cn;
+  phase_sincos(Pn, sn, cn);
+  rout[q] = make_uint4((uint32_t) (Xn >> 32), (uint32_t) (Yn >> 32), __float_as_uint(cn), __float_as_uint(sn));
+  aout[q] = make_uint4((uint32_t) Xn, (uint32_t) Yn, Pn, __float_as_uint(wi + dw));
+  // box crossings and phase turns are rare: read-modify-write only then
+  if (cx | cy)
+  {
+    const int2 im = B.img[q];
+    B.img[q] = make_int2(im.x + cx, im.y + cy);
+  }
+  if (ct) B.turns[q] += ct;
+  return fmaf(ddx, ddx, ddy * ddy);
+}
+
+// warp max of |dr|^2 for the Verlet trigger; a warp issues its atomic only
+// when it can raise the maximum already stored (no block barrier)
+__device__ __forceinline__ void publish_max(FastControl *ctrl, float d2max, int err)
+{
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) d2max = fmaxf(d2max, __shfl_xor_sync(0xffffffffu, d2max, off));
+  err = __any_sync(0xffffffffu, err);
+  if ((threadIdx.x & 31) == 0)
+  {
+    const unsigned bits = __float_as_uint(d2max);
+    if (bits > *(volatile unsigned *) &ctrl->max2_bits) atomicMax(&ctrl->max2_bits, bits);
+    if (err) atomicOr(&ctrl->error, 1);
+  }
+}
+
+// One SE or SRK step of one particle per thread, neighbours gathered from
+// global memory (all pairs; also usable for every kind).
 template<int MODEL, int STEPPER, int KIND>
 __global__ void __launch_bounds__(kTB, 4) fast_step_kernel(FastParams P, FastBuffers B)
 {
@@ -535,123 +896,119 @@ __global__ void __launch_bounds__(kTB, 4) fast_step_kernel(FastParams P, FastBuf
     const unsigned p = B.pid[q];
     const uint4 ri = rin[q];
     const uint4 ai = ain[q];
-    const int cnt = KIND == KIND_VERLET ? B.vl_cnt[q] : 0;
-    float2 v = make_float2(0.f, 0.f);
-    if (MODEL == 2) v = B.vel[q];
-    int2 im = B.img[q];
-    int turns = B.turns[q];
-    // the noise does not depend on the neighbours: drawing it first overlaps
-    // its arithmetic with the loads above (exactly the normals the stepper
-    // consumes, reference draw order)
-    constexpr int kNeed = MODEL == 1 ? (STEPPER == 1 ? 1 : 2) : (STEPPER == 1 ? 3 : 6);
+    const float2 v = MODEL == 2 ? B.vel[q] : make_float2(0.f, 0.f);
     float z[6];
-    {
-      NoiseKey nk;
-      nk.seed = P.seed;
-      nk.replica = P.replica;
-      nk.step = ctrl->step;
-      const uint4 u = philox_block(nk, p, 0);
-      box_muller_f32(u.x, u.y, z[0], z[1]);
-      if (kNeed > 2) box_muller_f32(u.z, u.w, z[2], z[3]);
-      if (kNeed > 4)
-      {
-        const uint4 u1 = philox_block(nk, p, 1);
-        box_muller_f32(u1.x, u1.y, z[4], z[5]);
-      }
-    }
-    const uint64_t Xi = join64(ri.x, ai.x), Yi = join64(ri.y, ai.y);
-    const float cphi = __uint_as_float(ri.z), sphi = __uint_as_float(ri.w);
-    const float wi = __uint_as_float(ai.w);
+    draw_noise<MODEL, STEPPER>(P, ctrl->step, p, z);  // overlaps the loads above
     Acc a{0.f, 0.f, 0.f, 0.f, 0};
-    gather_sums<KIND, STEPPER == 2>(P, B, rin, ain, q, cnt, ri, Xi, Yi, a);
-    float f_w = 0.0f, C = 0.0f;  // SE/SRK zero-fill the derivative: an isolated particle keeps 0
-    if (a.card > 0)
-    {
-      const float inv = 1.0f / (float) a.card;
-      const float S = cphi * a.ss - sphi * a.sc;  // sum sin(phi_j - phi_i)
-      const float K = cphi * a.sc + sphi * a.ss;  // sum cos(phi_j - phi_i)
-      f_w = -P.xi_phi * wi + P.sigma * (P.ca * S - P.sa * K) * inv;
-      if (STEPPER == 2)
-      {
-        const float WS = cphi * a.ws - sphi * a.wc;  // sum omega_j sin(phi_j - phi_i)
-        const float WK = cphi * a.wc + sphi * a.ws;  // sum omega_j cos(phi_j - phi_i)
-        C = P.sigma * inv * ((P.ca * WK + P.sa * WS) - wi * (P.ca * K + P.sa * S));
-      }
-    }
-    const float dt = P.dt;
-    float ddx, ddy, dphi, dw;
-    const int2 im0 = im;
-    const int turns0 = turns;
-    if (MODEL == 1)
-    {
-      const float fx = P.v0 * cphi, fy = P.v0 * sphi, fp = wi;
-      if (STEPPER == 1)
-      {
-        // StochasticEulerStepperPtr.hpp:58-66
-        ddx = fx * dt;
-        ddy = fy * dt;
-        dphi = fp * dt;
-        dw = f_w * dt + P.b_phi * (P.sqdt * z[0]);
-      } else
-      {
-        // StochasticRungeKuttaStepperPtr.hpp:54-70
-        const float dW = z[0] * P.sqdt;
-        const float dZ = P.half_dt15 * (z[0] + P.inv_sqrt3 * z[1]);
-        ddx = fx * dt - fp * fy * P.half_dt2;
-        ddy = fy * dt + fp * fx * P.half_dt2;
-        dphi = fp * dt + f_w * P.half_dt2 + P.b_phi * dZ;
-        dw = f_w * dt + (C - P.xi * f_w) * P.half_dt2 + P.b_phi * (dW - P.xi * dZ);
-      }
-    } else
-    {
-      const float fvx = -P.xi_r * v.x + P.v0 * cphi, fvy = -P.xi_r * v.y + P.v0 * sphi;
-      float dvx, dvy;
-      if (STEPPER == 1)
-      {
-        // StochasticEulerStepper.hpp:44-50 with AddNoise (ParticleSystemSecondOrder.cpp:447-449)
-        ddx = dt * v.x;
-        ddy = dt * v.y;
-        dvx = dt * fvx + P.sqdt * (P.b_r * z[0]);
-        dvy = dt * fvy + P.sqdt * (P.b_r * z[1]);
-        dphi = dt * wi;
-        dw = dt * f_w + P.sqdt * (P.b_phi * z[2]);
-      } else
-      {
-        // second-order strong order 1.5 Taylor scheme (no reference code)
-        const float dWx = z[0] * P.sqdt, dZx = P.half_dt15 * (z[0] + P.inv_sqrt3 * z[1]);
-        const float dWy = z[2] * P.sqdt, dZy = P.half_dt15 * (z[2] + P.inv_sqrt3 * z[3]);
-        const float dWw = z[4] * P.sqdt, dZw = P.half_dt15 * (z[4] + P.inv_sqrt3 * z[5]);
-        ddx = v.x * dt + fvx * P.half_dt2 + P.b_r * dZx;
-        ddy = v.y * dt + fvy * P.half_dt2 + P.b_r * dZy;
-        dvx = fvx * dt + (-P.xi_r * fvx - P.v0 * sphi * wi) * P.half_dt2 + P.b_r * (dWx - P.xi_r * dZx);
-        dvy = fvy * dt + (-P.xi_r * fvy + P.v0 * cphi * wi) * P.half_dt2 + P.b_r * (dWy - P.xi_r * dZy);
-        dphi = wi * dt + f_w * P.half_dt2 + P.b_phi * dZw;
-        dw = f_w * dt + (C - P.xi_phi * f_w) * P.half_dt2 + P.b_phi * (dWw - P.xi_phi * dZw);
-      }
-      B.vel[q] = make_float2(v.x + dvx, v.y + dvy);
-    }
-    const uint64_t Xn = advance(Xi, fix64_of(ddx, err), im.x);
-    const uint64_t Yn = advance(Yi, fix64_of(ddy, err), im.y);
-    const uint32_t Pn = advance_phase(ai.z, dphi, turns, err);
-    float sn, cn;
-    phase_sincos(Pn, sn, cn);
-    rout[q] = make_uint4((uint32_t) (Xn >> 32), (uint32_t) (Yn >> 32), __float_as_uint(cn), __float_as_uint(sn));
-    aout[q] = make_uint4((uint32_t) Xn, (uint32_t) Yn, Pn, __float_as_uint(wi + dw));
-    if (im.x != im0.x || im.y != im0.y) B.img[q] = im;
-    if (turns != turns0) B.turns[q] = turns;
-    d2max = fmaf(ddx, ddx, ddy * ddy);
+    gather_sums<KIND, STEPPER == 2>(P, B, rin, ain, q, KIND == KIND_VERLET ? -1 : 0, nullptr, 0, ri,
+                                    join64(ri.x, ai.x), join64(ri.y, ai.y), a);
+    d2max = update_particle<MODEL, STEPPER>(P, B, q, ri, ai, v, a, z, rout, aout, err);
   }
-  // warp max of |dr|^2 for the Verlet trigger; a warp issues its atomic only
-  // when it can raise the maximum already stored (no block barrier)
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) d2max = fmaxf(d2max, __shfl_xor_sync(0xffffffffu, d2max, off));
-  err = __any_sync(0xffffffffu, err);
-  if ((threadIdx.x & 31) == 0)
+  publish_max(ctrl, d2max, err);
+}
+
+// One SE or SRK step of one tile per CTA with the neighbourhood staged in
+// shared memory by TMA bulk copies (cp.async.bulk, completion on an mbarrier).
+template<int MODEL, int STEPPER, int KIND>
+__global__ void __launch_bounds__(kTileThreads, 8) fast_tile_kernel(FastParams P, FastBuffers B)
+{
+  __shared__ __align__(16) uint4 srec[kTileCap];
+  __shared__ __align__(16) uint4 saux[kTileCap];
+  __shared__ __align__(16) short slist[KIND == KIND_VERLET ? kListCap : 8];
+  __shared__ __align__(8) unsigned long long mbar;
+  __shared__ TileLayout L;
+  __shared__ int list_staged, list_stride;
+  FastControl *ctrl = B.ctrl;
+  const int par = ctrl->parity;
+  const uint4 *rin = par ? B.rec1 : B.rec0;
+  const uint4 *ain = par ? B.aux1 : B.aux0;
+  uint4 *rout = par ? B.rec0 : B.rec1;
+  uint4 *aout = par ? B.aux0 : B.aux1;
+  const short *glist = nullptr;  // this tile's list rows in global memory
+  if (threadIdx.x == 0)
   {
-    const unsigned bits = __float_as_uint(d2max);
-    if (bits > *(volatile unsigned *) &ctrl->max2_bits) atomicMax(&ctrl->max2_bits, bits);
-    if (err) atomicOr(&ctrl->error, 1);
+    L = reinterpret_cast<const TileLayout *>(B.tiles)[blockIdx.x];
+    if (L.p_end <= L.p_begin) L.staged = 0;
+    list_stride = tile_list_stride(L.p_begin, L.p_end);
+    const int rows = KIND == KIND_VERLET ? B.tile_maxcnt[blockIdx.x] : 0;
+    const uint32_t list_bytes = 2u * (uint32_t) rows * (uint32_t) list_stride;
+    list_staged = L.staged && KIND == KIND_VERLET && rows > 0 && rows * list_stride <= kListCap;
+    if (L.staged)
+    {
+      const uint32_t mb = smem_u32(&mbar);
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      const uint32_t tx = 32u * L.total + (list_staged ? list_bytes : 0u);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(tx) : "memory");
+      for (int k = 0; k < L.nseg; ++k)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(&srec[L.base[k]])),
+                     "l"(rin + L.start[k]), "r"(16u * L.len[k]), "r"(mb)
+                     : "memory");
+      for (int k = 0; k < L.nseg; ++k)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(&saux[L.base[k]])),
+                     "l"(ain + L.start[k]), "r"(16u * L.len[k]), "r"(mb)
+                     : "memory");
+      if (list_staged)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(slist)),
+                     "l"(B.vl + tile_list_base(P.cap, blockIdx.x, L.p_begin)), "r"(list_bytes), "r"(mb)
+                     : "memory");
+    }
   }
+  __syncthreads();
+  const bool staged = L.staged;
+  if (L.p_end <= L.p_begin) return;
+  if (KIND == KIND_VERLET) glist = B.vl + tile_list_base(P.cap, blockIdx.x, L.p_begin);
+  if (staged)
+  {
+    // wait for the bulk copies (phase 0), bounded in time
+    const uint32_t mb = smem_u32(&mbar);
+    uint32_t done = 0;
+    long long t0 = clock64();
+    while (!done && clock64() - t0 < kWaitCycles)
+      asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}"
+                   : "=r"(done)
+                   : "r"(mb)
+                   : "memory");
+    if (!__syncthreads_and(done))
+    {
+      // the copies did not complete in time: report, give them a second bounded
+      // wait so none is in flight when the CTA exits, and leave this tile
+      if (threadIdx.x == 0) atomicOr(&ctrl->error, 2);
+      t0 = clock64();
+      while (!done && clock64() - t0 < kWaitCycles)
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(mb)
+            : "memory");
+      return;
+    }
+  }
+  float d2max = 0.0f;
+  int err = 0;
+  for (int q = L.p_begin + threadIdx.x; q < L.p_end; q += blockDim.x)
+  {
+    const unsigned p = B.pid[q];
+    const uint4 ri = rin[q];
+    const uint4 ai = ain[q];
+    const int cnt = KIND == KIND_VERLET ? B.vl_cnt[q] : 0;
+    const float2 v = MODEL == 2 ? B.vel[q] : make_float2(0.f, 0.f);
+    float z[6];
+    draw_noise<MODEL, STEPPER>(P, ctrl->step, p, z);
+    Acc a{0.f, 0.f, 0.f, 0.f, 0};
+    const uint64_t Xi = join64(ri.x, ai.x), Yi = join64(ri.y, ai.y);
+    const int i = q - L.p_begin;
+    const short *lp = KIND == KIND_VERLET ? (list_staged ? slist + i : glist + i) : nullptr;
+    if (staged)
+      gather_sums_staged<KIND, STEPPER == 2>(P, B, srec, saux, L, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
+    else
+      gather_sums<KIND, STEPPER == 2>(P, B, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
+    d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(P, B, q, ri, ai, v, a, z, rout, aout, err));
+  }
+  publish_max(ctrl, d2max, err);
 }
 
 // After a step: advance the noise counter and the buffer parity, accumulate
@@ -731,6 +1088,8 @@ static FastBuffers buffers(spss_ctx *ctx)
   B.order = f->binner.members.ptr;
   B.vl = f->vl.ptr;
   B.vl_cnt = f->vl_cnt.ptr;
+  B.tile_maxcnt = f->tile_maxcnt.ptr;
+  B.tiles = f->tiles.ptr;
   B.ctrl = f->ctrl;
   return B;
 }
@@ -757,11 +1116,14 @@ static FastParams params(spss_ctx *ctx, double dt)
   P.sa = (float) std::sin(p.alpha);
   const double rho2 = p.rho * p.rho;
   P.rho2_d = rho2;
-  P.rho2_f = (float) rho2;
+  // FP32 pair distances are squared differences of the 32-bit position words,
+  // i.e. in units of 2^-64 of the box area
+  const double area = 18446744073709551616.0;
+  P.rho2_f = (float) (rho2 * area);
   // |d2_f - d2| <= 2 (|dx| + |dy|) 2^-32 + 2^-32 + 4 d2 2^-24 near r = rho; doubled
-  P.band_f = (float) (2.0 * (4.0 * p.rho * 2.3283064365386963e-10 + 2.3283064365386963e-10 + 4.0 * rho2 * 5.9604644775390625e-8));
+  P.band_f = (float) (area * 2.0 * (4.0 * p.rho * 2.3283064365386963e-10 + 2.3283064365386963e-10 + 4.0 * rho2 * 5.9604644775390625e-8));
   const double rmax2 = ctx->r_max * ctx->r_max;
-  P.rmax2_f = (float) (rmax2 + 2.0 * (4.0 * ctx->r_max * 2.3283064365386963e-10 + 4.0 * rmax2 * 5.9604644775390625e-8));
+  P.rmax2_f = (float) (area * (rmax2 + 2.0 * (4.0 * ctx->r_max * 2.3283064365386963e-10 + 4.0 * rmax2 * 5.9604644775390625e-8)));
   P.half_skin = 0.5 * (ctx->r_max - ctx->r_min);
   P.dt = (float) dt;
   P.sqdt = (float) std::sqrt(dt);
@@ -823,12 +1185,16 @@ int fast_create(spss_ctx *ctx)
   SPSS_TRY(f->cell_of.reserve(n));
   SPSS_TRY(f->cell_sorted.reserve(n));
   SPSS_TRY(f->vl_cnt.reserve(n));
+  if (f->kind != KIND_ALL_PAIRS)
+    SPSS_TRY(f->tiles.reserve(sizeof(TileLayout) * (size_t) f->nc_build * tiles_per_row(f->nc_build)));
   if (f->kind == KIND_VERLET)
   {
     // mean list length: pi r_max^2 n (unit box); room for six standard deviations
     const double lam = M_PI * ctx->r_max * ctx->r_max * n;
     f->cap = std::max(16, ((int) std::ceil(lam + 6.0 * std::sqrt(lam) + 8.0) + 3) & ~3);
-    SPSS_TRY(f->vl.reserve((size_t) f->cap * n));
+    const long ntiles = (long) f->nc_build * tiles_per_row(f->nc_build);
+    SPSS_TRY(f->vl.reserve((size_t) f->cap * ((size_t) n + 16 * (size_t) ntiles + 16)));
+    SPSS_TRY(f->tile_maxcnt.reserve((size_t) ntiles));
   }
   SPSS_CUDA_TRY(cudaMalloc((void **) &f->ctrl, sizeof(FastControl)));
   SPSS_CUDA_TRY(cudaMallocHost((void **) &f->h_ctrl, sizeof(FastControl)));
@@ -868,6 +1234,8 @@ void fast_destroy(spss_ctx *ctx)
   f->cell_sorted.release();
   f->vl.release();
   f->vl_cnt.release();
+  f->tile_maxcnt.release();
+  f->tiles.release();
   f->binner.release();
   if (f->ctrl) cudaFree(f->ctrl);
   if (f->h_ctrl) cudaFreeHost(f->h_ctrl);
@@ -898,8 +1266,16 @@ static int launch_rebuild(spss_ctx *ctx, const FastParams &P)
   fast_after_rebuild_kernel<<<1, 1, 0, ctx->stream>>>(f->ctrl, f->kind != KIND_ALL_PAIRS);
   ++ctx->launches;
   SPSS_TRY(check_launch("fast_after_rebuild_kernel"));
+  if (f->kind != KIND_ALL_PAIRS)
+  {
+    const int ntiles = P.nc * tiles_per_row(P.nc);
+    fast_tile_layout_kernel<<<blocks_for(ntiles, 128), 128, 0, ctx->stream>>>(P, buffers(ctx));
+    ++ctx->launches;
+    SPSS_TRY(check_launch("fast_tile_layout_kernel"));
+  }
   if (f->kind == KIND_VERLET)
   {
+    SPSS_CUDA_TRY(cudaMemsetAsync(f->tile_maxcnt.ptr, 0, sizeof(int) * f->tile_maxcnt.count, ctx->stream));
     fast_verlet_build_kernel<<<blocks_for(n, 128), 128, 0, ctx->stream>>>(P, buffers(ctx));
     ++ctx->launches;
     SPSS_TRY(check_launch("fast_verlet_build_kernel"));
@@ -911,11 +1287,14 @@ template<int MODEL, int STEPPER>
 static void launch_step_kind(spss_ctx *ctx, const FastParams &P, const FastBuffers &B)
 {
   const int grid = blocks_for(P.n, kTB);
+  const int tiles = P.nc * tiles_per_row(P.nc);
   switch (ctx->fast->kind)
   {
     case KIND_ALL_PAIRS: fast_step_kernel<MODEL, STEPPER, KIND_ALL_PAIRS><<<grid, kTB, 0, ctx->stream>>>(P, B); break;
-    case KIND_CELLS: fast_step_kernel<MODEL, STEPPER, KIND_CELLS><<<grid, kTB, 0, ctx->stream>>>(P, B); break;
-    default: fast_step_kernel<MODEL, STEPPER, KIND_VERLET><<<grid, kTB, 0, ctx->stream>>>(P, B); break;
+    case KIND_CELLS:
+      fast_tile_kernel<MODEL, STEPPER, KIND_CELLS><<<tiles, kTileThreads, 0, ctx->stream>>>(P, B);
+      break;
+    default: fast_tile_kernel<MODEL, STEPPER, KIND_VERLET><<<tiles, kTileThreads, 0, ctx->stream>>>(P, B); break;
   }
 }
 

@@ -7,7 +7,7 @@
 #include <cmath>
 #include <vector>
 
-#include "../../include/spss_gpu.h"
+#include "spss_gpu.h"
 
 namespace spss
 {
