@@ -143,7 +143,7 @@ def hbm_peak():
 def traffic_per_launch():
     """DRAM bytes per launch of the pair-and-update kernel from the committed
     ncu summary (profiles/), scaled to the full system; None before a capture."""
-    path = os.path.join(ROOT, "profiles", "fast_step_srk2_verlet.json")
+    path = os.path.join(ROOT, "profiles", "fast_tile_kernel_srk2_verlet.json")
     try:
         with open(path) as f:
             d = json.load(f)
@@ -313,7 +313,7 @@ def run_ours(args, rank, world, local_rank):
                        n * 56 / 1e6, n * 4 * (mean_list_length(p) + 1) / 1e6),
                    "parallelism": "replicas x%d" % world},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_kind": peak_kind, "kernel": "fast_step_kernel<2,2,2> (pair sums + SRK update)",
+                     "peak_kind": peak_kind, "kernel": "fast_tile_kernel<2,2,2> (pair sums + SRK update)",
                      "kernel_ms": avg_kernel_s * 1e3,
                      "algorithmic_bytes_per_particle": algorithmic_bytes_per_particle(p),
                      "traffic": None if traffic is None else traffic * n},
