@@ -169,6 +169,57 @@ int spss_get_timing(spss_ctx *ctx, double *kernel_ms, unsigned long long *timed_
  * SPSS_ERR_SIZE for n <= 0 or n > SPSS_NOALLOC_MAX_PARTICLES. */
 int spss_order_parameters_noalloc(int model, const double *state, long n, double *out4, void *cuda_stream);
 
+/* ------------------------------------------------------------------ batches
+ *
+ * A batch context steps `nsys` independent systems together — the GPU form of
+ * the reference's MPI parameter scan, where each rank runs its own parameter
+ * point (MPI_PARAMETER_SCAN in the SimulationEngine*Ptr engines): every kernel
+ * of a step (binning, lists, pair sums + update, trigger) serves all systems
+ * in one launch, and a step is one CUDA graph.  Systems may differ in every
+ * physical parameter (n, v0, xi, xi_r, D_r, xi_phi, D_phi, sigma, rho, alpha,
+ * r_max, nc_verlet, replica) but share model, flavor, variant, precision
+ * (SPSS_PRECISION_F32) and seed; system r draws the noise a single context with
+ * its parameters would draw.  State arrays (spss_set_state / spss_get_state /
+ * spss_noise) are the systems' AoS arrays concatenated in order.  The Verlet
+ * trigger is kept per system; when one system triggers, the lists of all are
+ * rebuilt.  No reference counterpart beyond the scan itself. */
+#define SPSS_MAX_SYSTEMS 65535
+int spss_batch_create(const spss_params *systems, int nsys, spss_ctx **out);
+/* Number of systems and (if `first` is not NULL) first[r] = index of system
+ * r's first particle, first[nsys] = all particles (nsys + 1 entries).  A
+ * single-system context reports one system. */
+int spss_batch_size(spss_ctx *ctx, int *nsys, long *first);
+/* Order parameters of every system, out[4 r + k] as spss_order_parameters
+ * (FP64 sums of the FP32 cos/sin of each phase and of the velocity directions);
+ * len = 4 nsys. */
+int spss_batch_order_parameters(spss_ctx *ctx, double *out, long len);
+/* nsteps steps (graph launches, no host synchronisation until the end).  After
+ * every step whose step counter (spss_get_step_counter) is a multiple of
+ * sample_every and at least sample_from, the order parameters of every system
+ * are added to its running averages; sample_every = 0 takes no samples. */
+int spss_batch_run(spss_ctx *ctx, int stepper, double t0, double dt, long nsteps, long sample_every,
+                   long sample_from);
+#define SPSS_STATS_PER_SYSTEM 5
+/* Time averages of every system: out[5 r + 0..4] = mean and variance of the
+ * phase order |<e^{i phi}>|, mean and variance of the velocity-direction order
+ * |<v/|v|>| (first order: the phase order again), number of samples;
+ * len = 5 nsys. */
+int spss_batch_stats(spss_ctx *ctx, double *out, long len);
+int spss_batch_reset_stats(spss_ctx *ctx);
+
+/* Tiling of the pair-and-update kernel: cells per tile (one row of a system's
+ * cell grid; 1 .. 4096) and launch form (0: one CTA per tile; 1: persistent,
+ * one wave of CTAs taking tiles from a work counter).  Results do not depend
+ * on the tiling; the lists are rebuilt before the next step.  F32 contexts. */
+int spss_set_tiling(spss_ctx *ctx, int tile_cells, int persistent);
+int spss_get_tiling(spss_ctx *ctx, int *tile_cells, int *persistent);
+/* Times `steps` steps of every tiling candidate (8, 16, 32, 64 cells per tile,
+ * both launch forms) on the context's current state, keeps the fastest and
+ * restores the state, step counter and trigger as they were (the lists are
+ * rebuilt before the next step; before the first step that leaves every
+ * result identical to an untuned run).  best_ms_per_step may be NULL. */
+int spss_autotune(spss_ctx *ctx, int stepper, double dt, int steps, double *best_ms_per_step);
+
 #ifdef __cplusplus
 }
 #endif

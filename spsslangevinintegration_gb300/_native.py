@@ -91,7 +91,18 @@ SIGNATURES = {
     "spss_get_timing": (_i, [_vp, _dp, P(_ull)]),
     # device pointers in, device pointer out, caller's stream
     "spss_order_parameters_noalloc": (_i, [_i, _vp, _l, _vp, _vp]),
+    "spss_batch_create": (_i, [P(Params), _i, P(_vp)]),
+    "spss_batch_size": (_i, [_vp, _ip, P(_l)]),
+    "spss_batch_order_parameters": (_i, [_vp, _dp, _l]),
+    "spss_batch_run": (_i, [_vp, _i, _d, _d, _l, _l, _l]),
+    "spss_batch_stats": (_i, [_vp, _dp, _l]),
+    "spss_batch_reset_stats": (_i, [_vp]),
+    "spss_set_tiling": (_i, [_vp, _i, _i]),
+    "spss_get_tiling": (_i, [_vp, _ip, _ip]),
+    "spss_autotune": (_i, [_vp, _i, _d, _i, _dp]),
 }
+
+STATS_PER_SYSTEM = 5
 
 
 def lib(path=None):

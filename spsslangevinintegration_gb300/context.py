@@ -7,17 +7,24 @@ import numpy as np
 from . import _native as N
 
 
+def make_params(model, n, rho, precision=N.PRECISION_F64, variant=N.VARIANT_DISPATCH, flavor=1, v0=0.0, xi=0.0,
+                xi_r=0.0, D_r=0.0, xi_phi=0.0, D_phi=0.0, sigma=0.0, alpha=0.0, r_max=0.0, nc_verlet=0, seed=0,
+                replica=0):
+    """spss_params of one system (reference parameter names, unit box)."""
+    return N.Params(int(model), flavor, int(n), variant, precision, nc_verlet, v0, xi, xi_r, D_r, xi_phi, D_phi, sigma,
+                    rho, alpha, r_max, seed, replica)
+
+
 class Context:
     """One particle system on the GPU: state, interaction routine, steppers."""
 
-    def __init__(self, model, n, rho, precision=N.PRECISION_F64, variant=N.VARIANT_DISPATCH, flavor=1, v0=0.0,
-                 xi=0.0, xi_r=0.0, D_r=0.0, xi_phi=0.0, D_phi=0.0, sigma=0.0, alpha=0.0, r_max=0.0, nc_verlet=0,
-                 seed=0, replica=0):
+    def __init__(self, model, n, rho, **kw):
         self.L = N.lib()
         self.model, self.n = int(model), int(n)
         self.s = 4 if self.model == 1 else 6
-        self.params = N.Params(self.model, flavor, self.n, variant, precision, nc_verlet, v0, xi, xi_r, D_r, xi_phi,
-                               D_phi, sigma, rho, alpha, r_max, seed, replica)
+        self.nsys = 1
+        self.first = np.array([0, self.n])
+        self.params = make_params(model, n, rho, **kw)
         h = ctypes.c_void_p()
         N.check(self.L.spss_create(ctypes.byref(self.params), ctypes.byref(h)), "spss_create")
         self.h = h
@@ -185,3 +192,68 @@ class Context:
         c = ctypes.c_ulonglong()
         N.check(self.L.spss_kernel_launches(self.h, ctypes.byref(c)), "spss_kernel_launches")
         return c.value
+
+    # -- tiling of the pair-and-update kernel (F32 contexts)
+    def set_tiling(self, tile_cells, persistent=False):
+        N.check(self.L.spss_set_tiling(self.h, int(tile_cells), int(bool(persistent))), "spss_set_tiling")
+
+    def tiling(self):
+        tc, pers = ctypes.c_int(), ctypes.c_int()
+        N.check(self.L.spss_get_tiling(self.h, ctypes.byref(tc), ctypes.byref(pers)), "spss_get_tiling")
+        return tc.value, bool(pers.value)
+
+    def autotune(self, stepper, dt, steps=5):
+        """Fastest tiling over trial steps; the state is restored.  Returns ms per step."""
+        ms = ctypes.c_double()
+        N.check(self.L.spss_autotune(self.h, stepper, dt, int(steps), ctypes.byref(ms)), "spss_autotune")
+        return ms.value
+
+    # -- per-system order parameters and their time averages (F32 contexts)
+    def system_order_parameters(self):
+        out = np.empty((self.nsys, 4))
+        N.check(self.L.spss_batch_order_parameters(self.h, N.dptr(out), out.size), "spss_batch_order_parameters")
+        return out
+
+    def run(self, stepper, t0, dt, nsteps, sample_every=0, sample_from=0):
+        N.check(self.L.spss_batch_run(self.h, stepper, t0, dt, int(nsteps), int(sample_every), int(sample_from)),
+                "spss_batch_run")
+
+    def stats(self):
+        """(nsys, 5): mean and variance of the phase order, mean and variance of
+        the velocity-direction order, number of samples."""
+        out = np.empty((self.nsys, N.STATS_PER_SYSTEM))
+        N.check(self.L.spss_batch_stats(self.h, N.dptr(out), out.size), "spss_batch_stats")
+        return out
+
+    def reset_stats(self):
+        N.check(self.L.spss_batch_reset_stats(self.h), "spss_batch_reset_stats")
+
+
+class Batch(Context):
+    """Independent systems stepped together (spss_batch_create); every
+    element of `systems` is a dict of make_params keywords.  State arrays are
+    the systems' AoS arrays concatenated in order (`first` holds the
+    particle offsets)."""
+
+    def __init__(self, systems):
+        self.L = N.lib()
+        plist = [make_params(**kw) for kw in systems]
+        arr = (N.Params * len(plist))(*plist)
+        self.model = int(plist[0].model)
+        self.s = 4 if self.model == 1 else 6
+        self.n = int(sum(p.n for p in plist))
+        self.params = plist[0]
+        self.systems = plist
+        h = ctypes.c_void_p()
+        N.check(self.L.spss_batch_create(arr, len(plist), ctypes.byref(h)), "spss_batch_create")
+        self.h = h
+        ns = ctypes.c_int()
+        N.check(self.L.spss_batch_size(self.h, ctypes.byref(ns), None), "spss_batch_size")
+        self.nsys = ns.value
+        first = (ctypes.c_long * (self.nsys + 1))()
+        N.check(self.L.spss_batch_size(self.h, ctypes.byref(ns), first), "spss_batch_size")
+        self.first = np.array(first[:], dtype=np.int64)
+
+    def system_rows(self, state, r):
+        """The AoS rows of system r in a concatenated state array."""
+        return state[self.s * self.first[r]: self.s * self.first[r + 1]]

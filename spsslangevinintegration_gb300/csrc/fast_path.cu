@@ -29,6 +29,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <utility>
 
 #include "spss_internal.cuh"
@@ -41,15 +42,38 @@ constexpr int kTB = 256;
 struct FastControl
 {
   unsigned long long step;  // Philox step counter of the next stochastic step
-  double acc;               // accumulated displacement (FP64)
+  double acc;               // accumulated displacement of system 0 (FP64)
   int parity;               // current rec/aux buffer
   int rebuild;              // lists (and slot order) rebuilt before the next evaluation
-  unsigned int max2_bits;   // max |dr|^2 of the step, FP32 bits (non-negative floats order as ints)
+  unsigned int unused;
   int overflow;             // largest Verlet count seen beyond capacity (0: none)
   int rebuilds;             // number of rebuilds performed
-  int error;                // bit 0: displacement too large for the fixed-point increment
+  int error;                // bit 0: displacement too large for the fixed-point increment; bit 1: staging timeout
   int uses_verlet;
+  int tile_next;            // work counter of the persistent tile kernel
+  long long sample_every;   // order-parameter samples after steps that are multiples of this (0: none)
+  long long sample_from;    // ... and not before this step
+};
+
+// Per-system Verlet trigger state (CalculateMaxDisplacement of each system).
+struct SysControl
+{
+  double acc;              // accumulated displacement (FP64)
+  unsigned int max2_bits;  // max |dr|^2 of the step, FP32 bits (non-negative floats order as ints)
   int pad;
+};
+
+// One independent system of a context (a context holds one or a batch of
+// them; each is the reference's particle system on its own unit box).  Its
+// particles are the slots [first, first + n) in every slot order, its cells
+// the global cells [cell0, cell0 + nc^2), its tiles [tile0, tile0 + ntiles).
+struct SysParams
+{
+  int n, first, nc, cell0;
+  int tile0, ntiles, index, replica;
+  float v0, xi, xi_r, xi_phi, sigma, ca, sa, rho2_f;
+  float band_f, rmax2_f, b_r, b_phi;
+  double rho2_d, half_skin;
 };
 
 enum Kind
@@ -59,10 +83,15 @@ enum Kind
   KIND_VERLET = 2
 };
 
+// Launch parameters: context-wide fields, plus the fields of one system
+// (nc .. replica), which kernels that work on several systems overwrite from
+// the system table (with_system).
 struct FastParams
 {
-  int n, nc, cap, model;
-  int kind, always_rebuild, pad0, pad1;
+  int n, nc, cap, model;      // n: slots of the whole context
+  int kind, always_rebuild, tile_cells, persistent;
+  int nsys, ntiles, first, sub_n;
+  int cell0, sys, pad0, pad1;
   float v0, xi, xi_r, xi_phi, sigma, ca, sa;
   float rho2_f, band_f, rmax2_f;
   double rho2_d, half_skin;
@@ -84,9 +113,46 @@ struct FastBuffers
   const int *order;
   short *vl;
   int *vl_cnt;
+  const SysParams *sys;  // system table
+  const int *sys_of;     // system of each slot (equivalently of each original index)
+  const int *tile_sys;   // system of each tile
+  SysControl *sysctl;
   int *tile_maxcnt;  // longest list of each tile (rows to stage)
   void *tiles;       // TileLayout of every tile, written at rebuild
   FastControl *ctrl;
+};
+
+// Device copy of the stepping state, for restoring it after trial steps.
+struct Snapshot
+{
+  DeviceArray<uint4> rec[2], aux[2];
+  DeviceArray<float2> vel;
+  DeviceArray<unsigned> pid, inv;
+  DeviceArray<int2> img;
+  DeviceArray<int> turns;
+  DeviceArray<SysControl> sysctl;
+  DeviceArray<FastControl> ctrl;
+  void release()
+  {
+    for (int b = 0; b < 2; ++b)
+    {
+      rec[b].release();
+      aux[b].release();
+    }
+    vel.release();
+    pid.release();
+    inv.release();
+    img.release();
+    turns.release();
+    sysctl.release();
+    ctrl.release();
+  }
+};
+
+// FP64 sums of one chunk of a system: cos phi, sin phi, v_x/|v|, v_y/|v|.
+struct __align__(16) OrderSums
+{
+  double c, s, vx, vy;
 };
 
 struct GraphEntry
@@ -106,6 +172,16 @@ struct FastPath
   DeviceArray<int> turns, turns_tmp, cell_of, cell_sorted, vl_cnt, tile_maxcnt;
   DeviceArray<short> vl;
   DeviceArray<unsigned char> tiles;
+  DeviceArray<SysParams> sys;
+  DeviceArray<int> sys_of, tile_sys;
+  DeviceArray<SysControl> sysctl;
+  std::vector<SysParams> h_sys;
+  int nsys = 1;
+  int total_cells = 1;
+  int ntiles = 0;
+  int tile_cells = 32;
+  int persistent = 0;
+  int persistent_grid = 0;
   Binner binner;
   FastControl *ctrl = nullptr;    // device
   FastControl *h_ctrl = nullptr;  // pinned mirror
@@ -114,7 +190,12 @@ struct FastPath
   int cap = 0;
   bool have_state = false;
   bool perm_valid = false;
-  std::map<std::pair<int, double>, GraphEntry> graphs;
+  std::map<std::tuple<int, double, int>, GraphEntry> graphs;  // (stepper, dt, with sampling)
+  // per-system order parameters and their time averages
+  DeviceArray<OrderSums> order_partial;
+  DeviceArray<double> order_out, stats;
+  int order_chunks = 1;
+  Snapshot snap;
 };
 
 // ---------------------------------------------------------------- helpers
@@ -122,6 +203,33 @@ struct FastPath
 __device__ __forceinline__ uint64_t join64(uint32_t hi, uint32_t lo)
 {
   return ((uint64_t) hi << 32) | lo;
+}
+
+// The launch parameters with the fields of system S.
+__device__ __forceinline__ FastParams with_system(const FastParams &P, const SysParams &S)
+{
+  FastParams Q = P;
+  Q.nc = S.nc;
+  Q.first = S.first;
+  Q.sub_n = S.n;
+  Q.cell0 = S.cell0;
+  Q.sys = S.index;
+  Q.v0 = S.v0;
+  Q.xi = S.xi;
+  Q.xi_r = S.xi_r;
+  Q.xi_phi = S.xi_phi;
+  Q.sigma = S.sigma;
+  Q.ca = S.ca;
+  Q.sa = S.sa;
+  Q.rho2_f = S.rho2_f;
+  Q.band_f = S.band_f;
+  Q.rmax2_f = S.rmax2_f;
+  Q.b_r = S.b_r;
+  Q.b_phi = S.b_phi;
+  Q.rho2_d = S.rho2_d;
+  Q.half_skin = S.half_skin;
+  Q.replica = (uint32_t) S.replica;
+  return Q;
 }
 
 // round-toward-zero f * 2^64 as a signed integer, exact for the 24-bit
@@ -373,7 +481,8 @@ __global__ void fast_cells_kernel(FastParams P, FastBuffers B)
   const int par = B.ctrl->parity;
   const uint4 r = (par ? B.rec1 : B.rec0)[q];
   const uint4 a = (par ? B.aux1 : B.aux0)[q];
-  B.cell_of[q] = cell_of_fix(join64(r.x, a.x), join64(r.y, a.y), P.nc);
+  const SysParams *S = B.sys + B.sys_of[q];
+  B.cell_of[q] = S->cell0 + cell_of_fix(join64(r.x, a.x), join64(r.y, a.y), S->nc);
 }
 
 // New slot q takes the particle of old slot order[q] (cells contiguous,
@@ -415,15 +524,15 @@ __global__ void fast_after_rebuild_kernel(FastControl *ctrl, int permuted)
 
 // ---------------------------------------------------------------- tiles
 //
-// A tile is a run of kTileCells cells of one row of the rebuild grid; one CTA
-// steps the particles of a tile.  Slots are sorted by cell, so the tile's
-// particles are one slot range and the records of its 3 x (kTileCells + 2)
+// A tile is a run of tile_cells cells of one row of a system's rebuild grid;
+// one CTA steps the particles of a tile.  Slots are sorted by cell, so the tile's
+// particles are one slot range and the records of its 3 x (tile_cells + 2)
 // neighbour cells are at most six slot segments (three rows, each split in
 // two where the periodic x-wrap crosses the row end).  The CTA stages those
 // segments into shared memory with TMA bulk copies; the Verlet list of a
 // particle in a staged tile stores shared-memory indices directly.
 
-constexpr int kTileCells = 32;    // cells per tile
+constexpr int kTileCellsDefault = 32;  // cells per tile unless tuned
 constexpr int kTileCap = 512;     // staged neighbour records per CTA (2 x 8 KiB)
 constexpr int kTileThreads = 128;
 constexpr long long kWaitCycles = 1ll << 31;  // about one second at the SM clock
@@ -436,17 +545,18 @@ struct TileLayout
   int staged;          // the neighbourhood fits kTileCap records
 };
 
-__host__ __device__ __forceinline__ int tiles_per_row(int nc)
+__host__ __device__ __forceinline__ int tiles_per_row(int nc, int tc)
 {
-  return (nc + kTileCells - 1) / kTileCells;
+  return (nc + tc - 1) / tc;
 }
 
-// Deterministic layout of tile t (the list build and the step compute the same).
-__device__ void tile_layout(int t, int nc, const int *__restrict__ off, TileLayout &L)
+// Deterministic layout of tile t of a system (cell offsets `off` of that
+// system's grid; the list build and the step compute the same).
+__device__ void tile_layout(int t, int nc, int tc, const int *__restrict__ off, TileLayout &L)
 {
-  const int nbx = tiles_per_row(nc);
+  const int nbx = tiles_per_row(nc, tc);
   const int cy = t / nbx, bx = t - cy * nbx;
-  const int cx_lo = bx * kTileCells, cx_hi = min(nc, cx_lo + kTileCells);
+  const int cx_lo = bx * tc, cx_hi = min(nc, cx_lo + tc);
   L.p_begin = off[cy * nc + cx_lo];
   L.p_end = off[cy * nc + cx_hi];
   L.nseg = 0;
@@ -505,19 +615,20 @@ __device__ void tile_layout(int t, int nc, const int *__restrict__ off, TileLayo
   L.staged = L.total <= kTileCap;
 }
 
-__device__ __forceinline__ int tile_of_cell(int c, int nc)
+__device__ __forceinline__ int tile_of_cell(int c, int nc, int tc)
 {
   const int cy = c / nc;
-  return cy * tiles_per_row(nc) + (c - cy * nc) / kTileCells;
+  return cy * tiles_per_row(nc, tc) + (c - cy * nc) / tc;
 }
 
-// Layout of every tile of the rebuild grid, once per rebuild.
+// Layout of every tile of every system, once per rebuild.
 __global__ void fast_tile_layout_kernel(FastParams P, FastBuffers B)
 {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= P.nc * tiles_per_row(P.nc)) return;
+  if (t >= P.ntiles) return;
+  const SysParams *S = B.sys + B.tile_sys[t];
   TileLayout L;
-  tile_layout(t, P.nc, B.cell_off, L);
+  tile_layout(t - S->tile0, S->nc, P.tile_cells, B.cell_off + S->cell0, L);
   reinterpret_cast<TileLayout *>(B.tiles)[t] = L;
 }
 
@@ -572,9 +683,13 @@ __global__ void fast_verlet_build_kernel(FastParams P, FastBuffers B)
   const int par = B.ctrl->parity;
   const uint4 *rec = par ? B.rec1 : B.rec0;
   const uint4 ri = rec[q];
-  const int c = B.cell_sorted[q];
-  const int cx = c % P.nc, cy = c / P.nc;
-  const int t = tile_of_cell(c, P.nc);
+  const SysParams *S = B.sys + B.sys_of[q];
+  const int nc = S->nc;
+  const float rmax2_f = S->rmax2_f;
+  const int *coff = B.cell_off + S->cell0;
+  const int c = B.cell_sorted[q] - S->cell0;
+  const int cx = c % nc, cy = c / nc;
+  const int t = S->tile0 + tile_of_cell(c, nc, P.tile_cells);
   const TileLayout L = reinterpret_cast<const TileLayout *>(B.tiles)[t];
   int cnt = 0;
   bool far = false;
@@ -582,18 +697,18 @@ __global__ void fast_verlet_build_kernel(FastParams P, FastBuffers B)
   short *lp = B.vl + tile_list_base(P.cap, t, L.p_begin) + (q - L.p_begin);
   for (int sy = -1; sy <= 1; ++sy)
   {
-    const int jy = wrap_cell(cy + sy, P.nc);
+    const int jy = wrap_cell(cy + sy, nc);
     for (int sx = -1; sx <= 1; ++sx)
     {
-      const int jc = jy * P.nc + wrap_cell(cx + sx, P.nc);
-      const int e = B.cell_off[jc + 1];
-      for (int j = B.cell_off[jc]; j < e; ++j)
+      const int jc = jy * nc + wrap_cell(cx + sx, nc);
+      const int e = coff[jc + 1];
+      for (int j = coff[jc]; j < e; ++j)
       {
         if (j == q) continue;
         const uint4 rj = __ldg(&rec[j]);
         const float dx = (float) (int) (rj.x - ri.x);
         const float dy = (float) (int) (rj.y - ri.y);
-        if (fmaf(dx, dx, dy * dy) <= P.rmax2_f)
+        if (fmaf(dx, dx, dy * dy) <= rmax2_f)
         {
           int entry;
           if (L.staged)
@@ -654,11 +769,13 @@ __device__ __forceinline__ void gather_sums(const FastParams &P, const FastBuffe
   }
   if (KIND == KIND_ALL_PAIRS)
   {
-    for (int j = 0; j < P.n; ++j)
+    const int end = P.first + P.sub_n;
+    for (int j = P.first; j < end; ++j)
       if (j != q) candidate<OMEGA>(P, ri, Xi, Yi, rec, aux, j, a);
     return;
   }
-  const int c = B.cell_sorted[q];
+  const int *coff = B.cell_off + P.cell0;
+  const int c = B.cell_sorted[q] - P.cell0;
   const int cx = c % P.nc, cy = c / P.nc;
   // stencil in the reference's order (-1,-1),(0,-1),(1,-1),(-1,0),... (ParticleSystemFirstOrder.cpp:47-52)
   for (int sy = -1; sy <= 1; ++sy)
@@ -667,8 +784,8 @@ __device__ __forceinline__ void gather_sums(const FastParams &P, const FastBuffe
     for (int sx = -1; sx <= 1; ++sx)
     {
       const int jc = jy * P.nc + wrap_cell(cx + sx, P.nc);
-      const int e = B.cell_off[jc + 1];
-      for (int j = B.cell_off[jc]; j < e; ++j)
+      const int e = coff[jc + 1];
+      for (int j = coff[jc]; j < e; ++j)
         if (j != q) candidate<OMEGA>(P, ri, Xi, Yi, rec, aux, j, a);
     }
   }
@@ -725,7 +842,8 @@ __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const Fa
   }
   // cell list, or a Verlet list that did not fit: scan the stencil of the
   // (rebuild-time) cell; each stencil cell is one contiguous staged range
-  const int c = B.cell_sorted[q];
+  const int *coff = B.cell_off + P.cell0;
+  const int c = B.cell_sorted[q] - P.cell0;
   const int cx = c % P.nc, cy = c / P.nc;
   for (int sy = -1; sy <= 1; ++sy)
   {
@@ -733,7 +851,7 @@ __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const Fa
     for (int sx = -1; sx <= 1; ++sx)
     {
       const int jc = jy * P.nc + wrap_cell(cx + sx, P.nc);
-      const int b = B.cell_off[jc], e = B.cell_off[jc + 1];
+      const int b = coff[jc], e = coff[jc + 1];
       if (e <= b) continue;
       const int i0 = staged_index(L, b);
       if (i0 < 0 || i0 + (e - b) > L.total)
@@ -759,6 +877,7 @@ __device__ __forceinline__ void draw_noise(const FastParams &P, unsigned long lo
   nk.seed = P.seed;
   nk.replica = P.replica;
   nk.step = step;
+  p -= (unsigned) P.first;  // index of the particle within its system
   const uint4 u = philox_block(nk, p, 0);
   box_muller_f32(u.x, u.y, z[0], z[1]);
   if (kNeed > 2) box_muller_f32(u.z, u.w, z[2], z[3]);
@@ -779,70 +898,77 @@ __device__ __forceinline__ float update_particle(const FastParams &P, const Fast
   const uint64_t Xi = join64(ri.x, ai.x), Yi = join64(ri.y, ai.y);
   const float cphi = __uint_as_float(ri.z), sphi = __uint_as_float(ri.w);
   const float wi = __uint_as_float(ai.w);
+  // Every rounding step is spelled out (fmaf, __fmul_rn, __fadd_rn): the
+  // compiler cannot contract or reassociate, so each instantiation of this
+  // function (one system or a batch) rounds identically.
   // sum sin(phi_j - phi_i - alpha) and sum (omega_j - omega_i) cos(phi_j - phi_i - alpha)
   float f_w = 0.0f, C = 0.0f;  // SE/SRK zero-fill the derivative: an isolated particle keeps 0
   if (a.card > 0)
   {
     const float inv = 1.0f / (float) a.card;
-    const float S = cphi * a.ss - sphi * a.sc;  // sum sin(phi_j - phi_i)
-    const float K = cphi * a.sc + sphi * a.ss;  // sum cos(phi_j - phi_i)
-    f_w = -P.xi_phi * wi + P.sigma * (P.ca * S - P.sa * K) * inv;
+    const float S = fmaf(cphi, a.ss, -__fmul_rn(sphi, a.sc));  // sum sin(phi_j - phi_i)
+    const float K = fmaf(cphi, a.sc, __fmul_rn(sphi, a.ss));   // sum cos(phi_j - phi_i)
+    f_w = fmaf(-P.xi_phi, wi, __fmul_rn(__fmul_rn(P.sigma, fmaf(P.ca, S, -__fmul_rn(P.sa, K))), inv));
     if (STEPPER == 2)
     {
-      const float WS = cphi * a.ws - sphi * a.wc;  // sum omega_j sin(phi_j - phi_i)
-      const float WK = cphi * a.wc + sphi * a.ws;  // sum omega_j cos(phi_j - phi_i)
-      C = P.sigma * inv * ((P.ca * WK + P.sa * WS) - wi * (P.ca * K + P.sa * S));
+      const float WS = fmaf(cphi, a.ws, -__fmul_rn(sphi, a.wc));  // sum omega_j sin(phi_j - phi_i)
+      const float WK = fmaf(cphi, a.wc, __fmul_rn(sphi, a.ws));   // sum omega_j cos(phi_j - phi_i)
+      C = __fmul_rn(__fmul_rn(P.sigma, inv), __fsub_rn(fmaf(P.ca, WK, __fmul_rn(P.sa, WS)),
+                                                       __fmul_rn(wi, fmaf(P.ca, K, __fmul_rn(P.sa, S)))));
     }
   }
   const float dt = P.dt;
   float ddx, ddy, dphi, dw;
   if (MODEL == 1)
   {
-    const float fx = P.v0 * cphi, fy = P.v0 * sphi, fp = wi;
+    const float fx = __fmul_rn(P.v0, cphi), fy = __fmul_rn(P.v0, sphi), fp = wi;
     if (STEPPER == 1)
     {
       // StochasticEulerStepperPtr.hpp:58-66
-      ddx = fx * dt;
-      ddy = fy * dt;
-      dphi = fp * dt;
-      dw = f_w * dt + P.b_phi * (P.sqdt * z[0]);
+      ddx = __fmul_rn(fx, dt);
+      ddy = __fmul_rn(fy, dt);
+      dphi = __fmul_rn(fp, dt);
+      dw = fmaf(f_w, dt, __fmul_rn(P.b_phi, __fmul_rn(P.sqdt, z[0])));
     } else
     {
       // StochasticRungeKuttaStepperPtr.hpp:54-70
-      const float dW = z[0] * P.sqdt;
-      const float dZ = P.half_dt15 * (z[0] + P.inv_sqrt3 * z[1]);
-      ddx = fx * dt - fp * fy * P.half_dt2;
-      ddy = fy * dt + fp * fx * P.half_dt2;
-      dphi = fp * dt + f_w * P.half_dt2 + P.b_phi * dZ;
-      dw = f_w * dt + (C - P.xi * f_w) * P.half_dt2 + P.b_phi * (dW - P.xi * dZ);
+      const float dW = __fmul_rn(z[0], P.sqdt);
+      const float dZ = __fmul_rn(P.half_dt15, fmaf(P.inv_sqrt3, z[1], z[0]));
+      ddx = fmaf(fx, dt, -__fmul_rn(__fmul_rn(fp, fy), P.half_dt2));
+      ddy = fmaf(fy, dt, __fmul_rn(__fmul_rn(fp, fx), P.half_dt2));
+      dphi = fmaf(fp, dt, fmaf(f_w, P.half_dt2, __fmul_rn(P.b_phi, dZ)));
+      dw = fmaf(f_w, dt, fmaf(fmaf(-P.xi, f_w, C), P.half_dt2, __fmul_rn(P.b_phi, fmaf(-P.xi, dZ, dW))));
     }
   } else
   {
-    const float fvx = -P.xi_r * v.x + P.v0 * cphi, fvy = -P.xi_r * v.y + P.v0 * sphi;
+    const float fvx = fmaf(-P.xi_r, v.x, __fmul_rn(P.v0, cphi));
+    const float fvy = fmaf(-P.xi_r, v.y, __fmul_rn(P.v0, sphi));
     float dvx, dvy;
     if (STEPPER == 1)
     {
       // StochasticEulerStepper.hpp:44-50 with AddNoise (ParticleSystemSecondOrder.cpp:447-449)
-      ddx = dt * v.x;
-      ddy = dt * v.y;
-      dvx = dt * fvx + P.sqdt * (P.b_r * z[0]);
-      dvy = dt * fvy + P.sqdt * (P.b_r * z[1]);
-      dphi = dt * wi;
-      dw = dt * f_w + P.sqdt * (P.b_phi * z[2]);
+      ddx = __fmul_rn(dt, v.x);
+      ddy = __fmul_rn(dt, v.y);
+      dvx = fmaf(dt, fvx, __fmul_rn(P.sqdt, __fmul_rn(P.b_r, z[0])));
+      dvy = fmaf(dt, fvy, __fmul_rn(P.sqdt, __fmul_rn(P.b_r, z[1])));
+      dphi = __fmul_rn(dt, wi);
+      dw = fmaf(dt, f_w, __fmul_rn(P.sqdt, __fmul_rn(P.b_phi, z[2])));
     } else
     {
       // second-order strong order 1.5 Taylor scheme (no reference code)
-      const float dWx = z[0] * P.sqdt, dZx = P.half_dt15 * (z[0] + P.inv_sqrt3 * z[1]);
-      const float dWy = z[2] * P.sqdt, dZy = P.half_dt15 * (z[2] + P.inv_sqrt3 * z[3]);
-      const float dWw = z[4] * P.sqdt, dZw = P.half_dt15 * (z[4] + P.inv_sqrt3 * z[5]);
-      ddx = v.x * dt + fvx * P.half_dt2 + P.b_r * dZx;
-      ddy = v.y * dt + fvy * P.half_dt2 + P.b_r * dZy;
-      dvx = fvx * dt + (-P.xi_r * fvx - P.v0 * sphi * wi) * P.half_dt2 + P.b_r * (dWx - P.xi_r * dZx);
-      dvy = fvy * dt + (-P.xi_r * fvy + P.v0 * cphi * wi) * P.half_dt2 + P.b_r * (dWy - P.xi_r * dZy);
-      dphi = wi * dt + f_w * P.half_dt2 + P.b_phi * dZw;
-      dw = f_w * dt + (C - P.xi_phi * f_w) * P.half_dt2 + P.b_phi * (dWw - P.xi_phi * dZw);
+      const float dWx = __fmul_rn(z[0], P.sqdt), dZx = __fmul_rn(P.half_dt15, fmaf(P.inv_sqrt3, z[1], z[0]));
+      const float dWy = __fmul_rn(z[2], P.sqdt), dZy = __fmul_rn(P.half_dt15, fmaf(P.inv_sqrt3, z[3], z[2]));
+      const float dWw = __fmul_rn(z[4], P.sqdt), dZw = __fmul_rn(P.half_dt15, fmaf(P.inv_sqrt3, z[5], z[4]));
+      ddx = fmaf(v.x, dt, fmaf(fvx, P.half_dt2, __fmul_rn(P.b_r, dZx)));
+      ddy = fmaf(v.y, dt, fmaf(fvy, P.half_dt2, __fmul_rn(P.b_r, dZy)));
+      dvx = fmaf(fvx, dt, fmaf(fmaf(-P.xi_r, fvx, -__fmul_rn(__fmul_rn(P.v0, sphi), wi)), P.half_dt2,
+                               __fmul_rn(P.b_r, fmaf(-P.xi_r, dZx, dWx))));
+      dvy = fmaf(fvy, dt, fmaf(fmaf(-P.xi_r, fvy, __fmul_rn(__fmul_rn(P.v0, cphi), wi)), P.half_dt2,
+                               __fmul_rn(P.b_r, fmaf(-P.xi_r, dZy, dWy))));
+      dphi = fmaf(wi, dt, fmaf(f_w, P.half_dt2, __fmul_rn(P.b_phi, dZw)));
+      dw = fmaf(f_w, dt, fmaf(fmaf(-P.xi_phi, f_w, C), P.half_dt2, __fmul_rn(P.b_phi, fmaf(-P.xi_phi, dZw, dWw))));
     }
-    B.vel[q] = make_float2(v.x + dvx, v.y + dvy);
+    B.vel[q] = make_float2(__fadd_rn(v.x, dvx), __fadd_rn(v.y, dvy));
   }
   int cx, cy, ct;
   const uint64_t Xn = advance(Xi, fix64_of(ddx, err), cx);
@@ -851,7 +977,7 @@ __device__ __forceinline__ float update_particle(const FastParams &P, const Fast
   float sn, cn;
   phase_sincos(Pn, sn, cn);
   rout[q] = make_uint4((uint32_t) (Xn >> 32), (uint32_t) (Yn >> 32), __float_as_uint(cn), __float_as_uint(sn));
-  aout[q] = make_uint4((uint32_t) Xn, (uint32_t) Yn, Pn, __float_as_uint(wi + dw));
+  aout[q] = make_uint4((uint32_t) Xn, (uint32_t) Yn, Pn, __float_as_uint(__fadd_rn(wi, dw)));
   // box crossings and phase turns are rare: read-modify-write only then
   if (cx | cy)
   {
@@ -859,27 +985,37 @@ __device__ __forceinline__ float update_particle(const FastParams &P, const Fast
     B.img[q] = make_int2(im.x + cx, im.y + cy);
   }
   if (ct) B.turns[q] += ct;
-  return fmaf(ddx, ddx, ddy * ddy);
+  return fmaf(ddx, ddx, __fmul_rn(ddy, ddy));
 }
 
-// warp max of |dr|^2 for the Verlet trigger; a warp issues its atomic only
-// when it can raise the maximum already stored (no block barrier)
-__device__ __forceinline__ void publish_max(FastControl *ctrl, float d2max, int err)
+// max |dr|^2 of each system for its Verlet trigger: a warp whose lanes all
+// belong to one system reduces first and issues one atomic, and only when it
+// can raise the maximum already stored (no block barrier).
+__device__ __forceinline__ void raise_max(SysControl *sc, float d2)
 {
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) d2max = fmaxf(d2max, __shfl_xor_sync(0xffffffffu, d2max, off));
-  err = __any_sync(0xffffffffu, err);
-  if ((threadIdx.x & 31) == 0)
+  const unsigned bits = __float_as_uint(d2);
+  if (bits > *(volatile unsigned *) &sc->max2_bits) atomicMax(&sc->max2_bits, bits);
+}
+
+__device__ __forceinline__ void publish_max(FastControl *ctrl, SysControl *sysctl, int sys, float d2max, int err)
+{
+  const int sys0 = __shfl_sync(0xffffffffu, sys, 0);
+  if (__all_sync(0xffffffffu, sys == sys0))
   {
-    const unsigned bits = __float_as_uint(d2max);
-    if (bits > *(volatile unsigned *) &ctrl->max2_bits) atomicMax(&ctrl->max2_bits, bits);
-    if (err) atomicOr(&ctrl->error, 1);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) d2max = fmaxf(d2max, __shfl_xor_sync(0xffffffffu, d2max, off));
+    if ((threadIdx.x & 31) == 0) raise_max(sysctl + sys0, d2max);
+  } else
+  {
+    raise_max(sysctl + sys, d2max);
   }
+  err = __any_sync(0xffffffffu, err);
+  if ((threadIdx.x & 31) == 0 && err) atomicOr(&ctrl->error, 1);
 }
 
 // One SE or SRK step of one particle per thread, neighbours gathered from
 // global memory (all pairs; also usable for every kind).
-template<int MODEL, int STEPPER, int KIND>
+template<int MODEL, int STEPPER, int KIND, bool MULTI>
 __global__ void __launch_bounds__(kTB, 4) fast_step_kernel(FastParams P, FastBuffers B)
 {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -891,25 +1027,112 @@ __global__ void __launch_bounds__(kTB, 4) fast_step_kernel(FastParams P, FastBuf
   uint4 *aout = par ? B.aux0 : B.aux1;
   float d2max = 0.0f;
   int err = 0;
+  int sys = 0;
   if (q < P.n)
   {
+    sys = MULTI ? B.sys_of[q] : 0;
+    const FastParams Q = MULTI ? with_system(P, B.sys[sys]) : P;
     const unsigned p = B.pid[q];
     const uint4 ri = rin[q];
     const uint4 ai = ain[q];
     const float2 v = MODEL == 2 ? B.vel[q] : make_float2(0.f, 0.f);
     float z[6];
-    draw_noise<MODEL, STEPPER>(P, ctrl->step, p, z);  // overlaps the loads above
+    draw_noise<MODEL, STEPPER>(Q, ctrl->step, p, z);  // overlaps the loads above
     Acc a{0.f, 0.f, 0.f, 0.f, 0};
-    gather_sums<KIND, STEPPER == 2>(P, B, rin, ain, q, KIND == KIND_VERLET ? -1 : 0, nullptr, 0, ri,
+    gather_sums<KIND, STEPPER == 2>(Q, B, rin, ain, q, KIND == KIND_VERLET ? -1 : 0, nullptr, 0, ri,
                                     join64(ri.x, ai.x), join64(ri.y, ai.y), a);
-    d2max = update_particle<MODEL, STEPPER>(P, B, q, ri, ai, v, a, z, rout, aout, err);
+    d2max = update_particle<MODEL, STEPPER>(Q, B, q, ri, ai, v, a, z, rout, aout, err);
   }
-  publish_max(ctrl, d2max, err);
+  publish_max(ctrl, B.sysctl, sys, d2max, err);
 }
 
-// One SE or SRK step of one tile per CTA with the neighbourhood staged in
-// shared memory by TMA bulk copies (cp.async.bulk, completion on an mbarrier).
+// Bounded wait for phase `phase` of an mbarrier (about one second).
+__device__ __forceinline__ uint32_t wait_phase(uint32_t mb, uint32_t phase)
+{
+  uint32_t done = 0;
+  const long long t0 = clock64();
+  while (!done && clock64() - t0 < kWaitCycles)
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(done)
+                 : "r"(mb), "r"(phase)
+                 : "memory");
+  return done;
+}
+
+// The particles of one tile, one per thread.
 template<int MODEL, int STEPPER, int KIND>
+__device__ __forceinline__ void step_tile(const FastParams &Q, const FastBuffers &B, const TileLayout &L,
+                                          const uint4 *srec, const uint4 *saux, const short *slist, const short *glist,
+                                          int list_staged, int list_stride, bool staged, const uint4 *rin,
+                                          const uint4 *ain, uint4 *rout, uint4 *aout, float &d2max, int &err)
+{
+  for (int q = L.p_begin + threadIdx.x; q < L.p_end; q += blockDim.x)
+  {
+    const unsigned p = B.pid[q];
+    const uint4 ri = rin[q];
+    const uint4 ai = ain[q];
+    const int cnt = KIND == KIND_VERLET ? B.vl_cnt[q] : 0;
+    const float2 v = MODEL == 2 ? B.vel[q] : make_float2(0.f, 0.f);
+    float z[6];
+    draw_noise<MODEL, STEPPER>(Q, B.ctrl->step, p, z);
+    Acc a{0.f, 0.f, 0.f, 0.f, 0};
+    const uint64_t Xi = join64(ri.x, ai.x), Yi = join64(ri.y, ai.y);
+    const int i = q - L.p_begin;
+    const short *lp = KIND == KIND_VERLET ? (list_staged ? slist + i : glist + i) : nullptr;
+    if (staged)
+      gather_sums_staged<KIND, STEPPER == 2>(Q, B, srec, saux, L, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
+    else
+      gather_sums<KIND, STEPPER == 2>(Q, B, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
+    d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, ri, ai, v, a, z, rout, aout, err));
+  }
+}
+
+// Staging of tile t by thread 0: layout, list geometry, and the bulk copies of
+// the neighbour records, aux words and list rows onto the mbarrier.
+template<int KIND>
+__device__ __forceinline__ void stage_tile(const FastParams &P, const FastBuffers &B, int t, const uint4 *rin,
+                                           const uint4 *ain, uint4 *srec, uint4 *saux, short *slist, uint32_t mb,
+                                           TileLayout &L, int &list_staged, int &list_stride, bool reuse)
+{
+  L = reinterpret_cast<const TileLayout *>(B.tiles)[t];
+  if (L.p_end <= L.p_begin) L.staged = 0;
+  list_stride = tile_list_stride(L.p_begin, L.p_end);
+  const int rows = KIND == KIND_VERLET ? B.tile_maxcnt[t] : 0;
+  const uint32_t list_bytes = 2u * (uint32_t) rows * (uint32_t) list_stride;
+  list_staged = L.staged && KIND == KIND_VERLET && rows > 0 && rows * list_stride <= kListCap;
+  if (!L.staged) return;
+  // generic-proxy reads of the buffers (previous tile) before async-proxy writes
+  if (reuse) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  const uint32_t tx = 32u * L.total + (list_staged ? list_bytes : 0u);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(tx) : "memory");
+  for (int k = 0; k < L.nseg; ++k)
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(&srec[L.base[k]])),
+                 "l"(rin + L.start[k]), "r"(16u * L.len[k]), "r"(mb)
+                 : "memory");
+  for (int k = 0; k < L.nseg; ++k)
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(&saux[L.base[k]])),
+                 "l"(ain + L.start[k]), "r"(16u * L.len[k]), "r"(mb)
+                 : "memory");
+  if (list_staged)
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(slist)),
+                 "l"(B.vl + tile_list_base(P.cap, t, L.p_begin)), "r"(list_bytes), "r"(mb)
+                 : "memory");
+}
+
+__device__ __forceinline__ void init_mbarrier(uint32_t mb)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// SE or SRK step of one tile per CTA with the neighbourhood staged in shared
+// memory by TMA bulk copies (cp.async.bulk, completion on an mbarrier).
+// MULTI: several systems, whose parameters come from the system table (one
+// system: from the kernel's parameter space, which costs no registers).
+template<int MODEL, int STEPPER, int KIND, bool MULTI>
 __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_kernel(FastParams P, FastBuffers B)
 {
   __shared__ __align__(16) uint4 srec[kTileCap];
@@ -924,69 +1147,31 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_kernel(FastParams P
   const uint4 *ain = par ? B.aux1 : B.aux0;
   uint4 *rout = par ? B.rec0 : B.rec1;
   uint4 *aout = par ? B.aux0 : B.aux1;
-  const short *glist = nullptr;  // this tile's list rows in global memory
+  const int t = blockIdx.x;
+  const uint32_t mb = smem_u32(&mbar);
   if (threadIdx.x == 0)
   {
-    L = reinterpret_cast<const TileLayout *>(B.tiles)[blockIdx.x];
-    if (L.p_end <= L.p_begin) L.staged = 0;
-    list_stride = tile_list_stride(L.p_begin, L.p_end);
-    const int rows = KIND == KIND_VERLET ? B.tile_maxcnt[blockIdx.x] : 0;
-    const uint32_t list_bytes = 2u * (uint32_t) rows * (uint32_t) list_stride;
-    list_staged = L.staged && KIND == KIND_VERLET && rows > 0 && rows * list_stride <= kListCap;
-    if (L.staged)
-    {
-      const uint32_t mb = smem_u32(&mbar);
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-      const uint32_t tx = 32u * L.total + (list_staged ? list_bytes : 0u);
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(tx) : "memory");
-      for (int k = 0; k < L.nseg; ++k)
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                         smem_u32(&srec[L.base[k]])),
-                     "l"(rin + L.start[k]), "r"(16u * L.len[k]), "r"(mb)
-                     : "memory");
-      for (int k = 0; k < L.nseg; ++k)
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                         smem_u32(&saux[L.base[k]])),
-                     "l"(ain + L.start[k]), "r"(16u * L.len[k]), "r"(mb)
-                     : "memory");
-      if (list_staged)
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                         smem_u32(slist)),
-                     "l"(B.vl + tile_list_base(P.cap, blockIdx.x, L.p_begin)), "r"(list_bytes), "r"(mb)
-                     : "memory");
-    }
+    init_mbarrier(mb);
+    stage_tile<KIND>(P, B, t, rin, ain, srec, saux, slist, mb, L, list_staged, list_stride, false);
   }
   __syncthreads();
   const bool staged = L.staged;
   if (L.p_end <= L.p_begin) return;
-  if (KIND == KIND_VERLET) glist = B.vl + tile_list_base(P.cap, blockIdx.x, L.p_begin);
+  const short *glist = KIND == KIND_VERLET ? B.vl + tile_list_base(P.cap, t, L.p_begin) : nullptr;
   if (staged)
   {
-    // wait for the bulk copies (phase 0), bounded in time
-    const uint32_t mb = smem_u32(&mbar);
-    uint32_t done = 0;
-    long long t0 = clock64();
-    while (!done && clock64() - t0 < kWaitCycles)
-      asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}"
-                   : "=r"(done)
-                   : "r"(mb)
-                   : "memory");
+    const uint32_t done = wait_phase(mb, 0);
     if (!__syncthreads_and(done))
     {
-      // the copies did not complete in time: report, give them a second bounded
-      // wait so none is in flight when the CTA exits, and leave this tile
+      // the copies did not complete in time: report, give them a second
+      // bounded wait so none is in flight when the CTA exits, and stop
       if (threadIdx.x == 0) atomicOr(&ctrl->error, 2);
-      t0 = clock64();
-      while (!done && clock64() - t0 < kWaitCycles)
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n selp.u32 %0, 1, 0, p;\n}"
-            : "=r"(done)
-            : "r"(mb)
-            : "memory");
+      wait_phase(mb, 0);
       return;
     }
   }
+  const int sys = MULTI ? B.tile_sys[t] : 0;
+  const FastParams Q = MULTI ? with_system(P, B.sys[sys]) : P;
   float d2max = 0.0f;
   int err = 0;
   for (int q = L.p_begin + threadIdx.x; q < L.p_end; q += blockDim.x)
@@ -997,43 +1182,120 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_kernel(FastParams P
     const int cnt = KIND == KIND_VERLET ? B.vl_cnt[q] : 0;
     const float2 v = MODEL == 2 ? B.vel[q] : make_float2(0.f, 0.f);
     float z[6];
-    draw_noise<MODEL, STEPPER>(P, ctrl->step, p, z);
+    draw_noise<MODEL, STEPPER>(Q, ctrl->step, p, z);
     Acc a{0.f, 0.f, 0.f, 0.f, 0};
     const uint64_t Xi = join64(ri.x, ai.x), Yi = join64(ri.y, ai.y);
     const int i = q - L.p_begin;
     const short *lp = KIND == KIND_VERLET ? (list_staged ? slist + i : glist + i) : nullptr;
     if (staged)
-      gather_sums_staged<KIND, STEPPER == 2>(P, B, srec, saux, L, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
+      gather_sums_staged<KIND, STEPPER == 2>(Q, B, srec, saux, L, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
     else
-      gather_sums<KIND, STEPPER == 2>(P, B, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
-    d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(P, B, q, ri, ai, v, a, z, rout, aout, err));
+      gather_sums<KIND, STEPPER == 2>(Q, B, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
+    d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, ri, ai, v, a, z, rout, aout, err));
   }
-  publish_max(ctrl, d2max, err);
+  publish_max(ctrl, B.sysctl, sys, d2max, err);
+}
+
+// The same step as a persistent launch: one wave of CTAs, each taking tiles
+// from a work counter until all tiles of all systems are done; the staging
+// buffers and the mbarrier (one phase per staged tile) are reused.
+template<int MODEL, int STEPPER, int KIND, bool MULTI>
+__global__ void __launch_bounds__(kTileThreads, 8) fast_tile_persistent_kernel(FastParams P, FastBuffers B)
+{
+  __shared__ __align__(16) uint4 srec[kTileCap];
+  __shared__ __align__(16) uint4 saux[kTileCap];
+  __shared__ __align__(16) short slist[KIND == KIND_VERLET ? kListCap : 8];
+  __shared__ __align__(8) unsigned long long mbar;
+  __shared__ TileLayout L;
+  __shared__ int list_staged, list_stride, tile_id;
+  __shared__ uint32_t phase;  // mbarrier phase of the next staged tile
+  FastControl *ctrl = B.ctrl;
+  const int par = ctrl->parity;
+  const uint4 *rin = par ? B.rec1 : B.rec0;
+  const uint4 *ain = par ? B.aux1 : B.aux0;
+  uint4 *rout = par ? B.rec0 : B.rec1;
+  uint4 *aout = par ? B.aux0 : B.aux1;
+  const uint32_t mb = smem_u32(&mbar);
+  if (threadIdx.x == 0)
+  {
+    init_mbarrier(mb);
+    phase = 0;
+  }
+  for (bool first = true;; first = false)
+  {
+    if (!first) __syncthreads();  // the previous tile's shared data is no longer read
+    if (threadIdx.x == 0)
+    {
+      const int t = atomicAdd(&ctrl->tile_next, 1);
+      tile_id = t;
+      if (t < P.ntiles)
+        stage_tile<KIND>(P, B, t, rin, ain, srec, saux, slist, mb, L, list_staged, list_stride, !first);
+    }
+    __syncthreads();
+    const int t = tile_id;
+    if (t >= P.ntiles) break;
+    const bool staged = L.staged;
+    if (staged)
+    {
+      const uint32_t ph = phase;
+      const uint32_t done = wait_phase(mb, ph);
+      if (!__syncthreads_and(done))
+      {
+        if (threadIdx.x == 0) atomicOr(&ctrl->error, 2);
+        wait_phase(mb, ph);
+        return;
+      }
+      if (threadIdx.x == 0) phase = ph ^ 1u;  // read again only after the next barrier
+    }
+    if (L.p_end <= L.p_begin) continue;
+    const int sys = MULTI ? B.tile_sys[t] : 0;
+    const short *glist = KIND == KIND_VERLET ? B.vl + tile_list_base(P.cap, t, L.p_begin) : nullptr;
+    float d2max = 0.0f;
+    int err = 0;
+    if (!MULTI)
+      step_tile<MODEL, STEPPER, KIND>(P, B, L, srec, saux, slist, glist, list_staged, list_stride, staged, rin, ain,
+                                      rout, aout, d2max, err);
+    else
+      step_tile<MODEL, STEPPER, KIND>(with_system(P, B.sys[sys]), B, L, srec, saux, slist, glist, list_staged,
+                                      list_stride, staged, rin, ain, rout, aout, d2max, err);
+    publish_max(ctrl, B.sysctl, sys, d2max, err);
+  }
 }
 
 // After a step: advance the noise counter and the buffer parity, accumulate
-// the displacement in FP64 and set the rebuild flag
-// (CalculateMaxDisplacement, ParticleSystemFirstOrder.cpp:670-696).
-__global__ void fast_control_kernel(FastControl *ctrl, double half_skin, int always_rebuild, int verlet)
+// each system's displacement in FP64 and set the rebuild flag
+// (CalculateMaxDisplacement, ParticleSystemFirstOrder.cpp:670-696).  The lists
+// of all systems are rebuilt together, so a rebuild restarts every system's
+// accumulator.  One block.
+__global__ void fast_control_kernel(FastControl *ctrl, SysControl *sysctl, const SysParams *sys, int nsys,
+                                    int always_rebuild, int verlet)
 {
-  ctrl->step += 1;
-  ctrl->parity ^= 1;
-  const double max2 = (double) __uint_as_float(ctrl->max2_bits);
-  ctrl->max2_bits = 0u;
-  if (always_rebuild)
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  for (int r = threadIdx.x; r < nsys; r += blockDim.x)
   {
-    ctrl->rebuild = 1;
-    return;
-  }
-  if (verlet)
-  {
-    ctrl->acc += sqrt(max2);
-    if (ctrl->acc > half_skin)
+    const double max2 = (double) __uint_as_float(sysctl[r].max2_bits);
+    sysctl[r].max2_bits = 0u;
+    if (verlet && !always_rebuild)
     {
-      ctrl->acc = 0.0;
-      ctrl->rebuild = 1;
+      const double acc = sysctl[r].acc + sqrt(max2);
+      sysctl[r].acc = acc;
+      if (acc > sys[r].half_skin) any = 1;
     }
   }
+  __syncthreads();
+  if (any)
+    for (int r = threadIdx.x; r < nsys; r += blockDim.x) sysctl[r].acc = 0.0;
+  if (threadIdx.x == 0)
+  {
+    ctrl->step += 1;
+    ctrl->parity ^= 1;
+    ctrl->tile_next = 0;
+    if (always_rebuild || any) ctrl->rebuild = 1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) ctrl->acc = sysctl[0].acc;
 }
 
 __global__ void fast_set_condition_kernel(const FastControl *ctrl, cudaGraphConditionalHandle handle)
@@ -1041,13 +1303,17 @@ __global__ void fast_set_condition_kernel(const FastControl *ctrl, cudaGraphCond
   cudaGraphSetConditional(handle, ctrl->rebuild ? 1u : 0u);
 }
 
-__global__ void fast_noise_kernel(double *__restrict__ out, int n, int per, NoiseKey nk)
+__global__ void fast_noise_kernel(double *__restrict__ out, int n, int per, NoiseKey nk, const SysParams *sys,
+                                  const int *sys_of)
 {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
+  const SysParams *S = sys + sys_of[p];
+  nk.replica = (uint32_t) S->replica;
+  const uint32_t local = (uint32_t) (p - S->first);
   float z[8];
-  normals4_f32(nk, (uint32_t) p, 0, z);
-  if (per > 4) normals4_f32(nk, (uint32_t) p, 1, z + 4);
+  normals4_f32(nk, local, 0, z);
+  if (per > 4) normals4_f32(nk, local, 1, z + 4);
   for (int d = 0; d < per; ++d) out[(long) per * p + d] = (double) z[d];
 }
 
@@ -1056,6 +1322,122 @@ __global__ void fast_pbc_kernel(int2 *img, int n)
 {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q < n) img[q] = make_int2(0, 0);
+}
+
+// ---------------------------------------------------------------- order parameters per system
+//
+// Phase order |<e^{i phi}>| and, for the second-order model, the polar order
+// of the velocity directions |<v/|v|>| of every system (the observers'
+// reduction, BinaryObserverFirstOrder.cpp:125-142, BinaryObserverSecondOrder.cpp:121-138),
+// summed in FP64 from the records of the current state.
+
+constexpr int kOrderChunk = 2048;  // slots per partial sum
+
+__device__ __forceinline__ bool sample_now(const FastControl *c)
+{
+  return c->sample_every > 0 && (long long) c->step >= c->sample_from && (long long) c->step % c->sample_every == 0;
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+// partial[sys * chunks + chunk] over the chunk's slots of system blockIdx.y;
+// `gated`: only after a sampling step (inside step graphs).
+__global__ void fast_order_partials_kernel(FastParams P, FastBuffers B, OrderSums *__restrict__ partial, int chunks,
+                                           int gated)
+{
+  if (gated && !sample_now(B.ctrl)) return;
+  __shared__ double sh[4][8];
+  const SysParams *S = B.sys + blockIdx.y;
+  const long begin = (long) S->first + (long) blockIdx.x * kOrderChunk;
+  const long end = min((long) S->first + S->n, begin + kOrderChunk);
+  const uint4 *rec = B.ctrl->parity ? B.rec1 : B.rec0;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  for (long q = begin + threadIdx.x; q < end; q += blockDim.x)
+  {
+    const uint4 r = rec[q];
+    a0 += (double) __uint_as_float(r.z);
+    a1 += (double) __uint_as_float(r.w);
+    if (P.model == 2)
+    {
+      const float2 v = B.vel[q];
+      const double vx = v.x, vy = v.y;
+      const double m = sqrt(vx * vx + vy * vy);
+      if (m > 0.0)
+      {
+        a2 += vx / m;
+        a3 += vy / m;
+      }
+    }
+  }
+  a0 = warp_sum(a0);
+  a1 = warp_sum(a1);
+  a2 = warp_sum(a2);
+  a3 = warp_sum(a3);
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if ((threadIdx.x & 31) == 0)
+  {
+    sh[0][w] = a0;
+    sh[1][w] = a1;
+    sh[2][w] = a2;
+    sh[3][w] = a3;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int k = 0; k < nw; ++k)
+      for (int c = 0; c < 4; ++c) t[c] += sh[c][k];
+    partial[(long) blockIdx.y * chunks + blockIdx.x] = OrderSums{t[0], t[1], t[2], t[3]};
+  }
+}
+
+// Per system: the order parameters (R, arg, R_v, arg_v) into out4 and, after a
+// sampling step, the running sums of R, R^2, R_v, R_v^2 and the sample count.
+__global__ void fast_order_finish_kernel(FastParams P, FastBuffers B, const OrderSums *__restrict__ partial, int chunks,
+                                         double *__restrict__ out4, double *__restrict__ stats, int gated)
+{
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= P.nsys) return;
+  if (gated && !sample_now(B.ctrl)) return;
+  double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+  for (int c = 0; c < chunks; ++c)
+  {
+    const OrderSums v = partial[(long) r * chunks + c];
+    t0 += v.c;
+    t1 += v.s;
+    t2 += v.vx;
+    t3 += v.vy;
+  }
+  const double n = (double) B.sys[r].n;
+  const double re = t0 / n, im = t1 / n;
+  double o[4];
+  o[0] = sqrt(re * re + im * im);
+  o[1] = atan2(im, re);
+  if (P.model == 2)
+  {
+    const double vre = t2 / n, vim = t3 / n;
+    o[2] = sqrt(vre * vre + vim * vim);
+    o[3] = atan2(vim, vre);
+  } else
+  {
+    o[2] = o[0];
+    o[3] = o[1];
+  }
+  for (int k = 0; k < 4; ++k) out4[4 * r + k] = o[k];
+  if (gated)
+  {
+    double *st = stats + 5 * r;
+    st[0] += o[0];
+    st[1] += o[0] * o[0];
+    st[2] += o[2];
+    st[3] += o[2] * o[2];
+    st[4] += 1.0;
+  }
 }
 
 // ---------------------------------------------------------------- host side
@@ -1090,51 +1472,141 @@ static FastBuffers buffers(spss_ctx *ctx)
   B.vl_cnt = f->vl_cnt.ptr;
   B.tile_maxcnt = f->tile_maxcnt.ptr;
   B.tiles = f->tiles.ptr;
+  B.sys = f->sys.ptr;
+  B.sys_of = f->sys_of.ptr;
+  B.tile_sys = f->tile_sys.ptr;
+  B.sysctl = f->sysctl.ptr;
   B.ctrl = f->ctrl;
   return B;
+}
+
+// Table entry of one system: its parameters in the FP32 / fixed-point units
+// of the kernels.
+static SysParams system_params(const spss_params &p, int index, int first, int nc, int cell0, int tile0,
+                               int ntiles, double r_min, double r_max)
+{
+  SysParams S;
+  std::memset(&S, 0, sizeof(S));
+  S.n = p.n;
+  S.first = first;
+  S.nc = nc;
+  S.cell0 = cell0;
+  S.tile0 = tile0;
+  S.ntiles = ntiles;
+  S.index = index;
+  S.replica = (int) p.replica;
+  S.v0 = (float) p.v0;
+  S.xi = (float) p.xi;
+  S.xi_r = (float) p.xi_r;
+  // first order: the torque friction is xi; second order: xi_phi
+  S.xi_phi = (float) (p.model == 1 ? p.xi : p.xi_phi);
+  S.sigma = (float) p.sigma;
+  S.ca = (float) std::cos(p.alpha);
+  S.sa = (float) std::sin(p.alpha);
+  const double rho2 = p.rho * p.rho;
+  S.rho2_d = rho2;
+  // FP32 pair distances are squared differences of the 32-bit position words,
+  // i.e. in units of 2^-64 of the box area
+  const double area = 18446744073709551616.0;
+  S.rho2_f = (float) (rho2 * area);
+  // |d2_f - d2| <= 2 (|dx| + |dy|) 2^-32 + 2^-32 + 4 d2 2^-24 near r = rho; doubled
+  S.band_f = (float) (area * 2.0 * (4.0 * p.rho * 2.3283064365386963e-10 + 2.3283064365386963e-10 + 4.0 * rho2 * 5.9604644775390625e-8));
+  const double rmax2 = r_max * r_max;
+  S.rmax2_f = (float) (area * (rmax2 + 2.0 * (4.0 * r_max * 2.3283064365386963e-10 + 4.0 * rmax2 * 5.9604644775390625e-8)));
+  S.half_skin = 0.5 * (r_max - r_min);
+  S.b_r = (float) std::sqrt(2.0 * p.D_r);
+  S.b_phi = (float) std::sqrt(2.0 * p.D_phi);
+  return S;
 }
 
 static FastParams params(spss_ctx *ctx, double dt)
 {
   const spss_params &p = ctx->p;
   FastPath *f = ctx->fast;
+  const SysParams &S = f->h_sys[0];
   FastParams P;
   std::memset(&P, 0, sizeof(P));
   P.n = p.n;
-  P.nc = f->nc_build;
   P.cap = f->cap;
   P.model = p.model;
   P.kind = f->kind;
   P.always_rebuild = f->kind == KIND_CELLS ? 1 : 0;
-  P.v0 = (float) p.v0;
-  P.xi = (float) p.xi;
-  P.xi_r = (float) p.xi_r;
-  // first order: the torque friction is xi; second order: xi_phi
-  P.xi_phi = (float) (p.model == 1 ? p.xi : p.xi_phi);
-  P.sigma = (float) p.sigma;
-  P.ca = (float) std::cos(p.alpha);
-  P.sa = (float) std::sin(p.alpha);
-  const double rho2 = p.rho * p.rho;
-  P.rho2_d = rho2;
-  // FP32 pair distances are squared differences of the 32-bit position words,
-  // i.e. in units of 2^-64 of the box area
-  const double area = 18446744073709551616.0;
-  P.rho2_f = (float) (rho2 * area);
-  // |d2_f - d2| <= 2 (|dx| + |dy|) 2^-32 + 2^-32 + 4 d2 2^-24 near r = rho; doubled
-  P.band_f = (float) (area * 2.0 * (4.0 * p.rho * 2.3283064365386963e-10 + 2.3283064365386963e-10 + 4.0 * rho2 * 5.9604644775390625e-8));
-  const double rmax2 = ctx->r_max * ctx->r_max;
-  P.rmax2_f = (float) (area * (rmax2 + 2.0 * (4.0 * ctx->r_max * 2.3283064365386963e-10 + 4.0 * rmax2 * 5.9604644775390625e-8)));
-  P.half_skin = 0.5 * (ctx->r_max - ctx->r_min);
+  P.tile_cells = f->tile_cells;
+  P.persistent = f->persistent;
+  P.nsys = f->nsys;
+  P.ntiles = f->ntiles;
+  // system 0 (kernels that serve several systems read theirs from the table)
+  P.nc = S.nc;
+  P.first = S.first;
+  P.sub_n = S.n;
+  P.cell0 = S.cell0;
+  P.v0 = S.v0;
+  P.xi = S.xi;
+  P.xi_r = S.xi_r;
+  P.xi_phi = S.xi_phi;
+  P.sigma = S.sigma;
+  P.ca = S.ca;
+  P.sa = S.sa;
+  P.rho2_f = S.rho2_f;
+  P.band_f = S.band_f;
+  P.rmax2_f = S.rmax2_f;
+  P.rho2_d = S.rho2_d;
+  P.half_skin = S.half_skin;
+  P.b_r = S.b_r;
+  P.b_phi = S.b_phi;
   P.dt = (float) dt;
   P.sqdt = (float) std::sqrt(dt);
   P.half_dt2 = (float) (0.5 * dt * dt);
   P.half_dt15 = (float) (0.5 * std::pow(dt, 1.5));
   P.inv_sqrt3 = (float) (1.0 / std::sqrt(3.0));
-  P.b_r = (float) std::sqrt(2.0 * p.D_r);
-  P.b_phi = (float) std::sqrt(2.0 * p.D_phi);
   P.seed = p.seed;
-  P.replica = p.replica;
+  P.replica = (uint32_t) S.replica;
   return P;
+}
+
+// Tile tables for a tile width (cells per tile); every system's tiles follow
+// the previous system's.
+static int set_tiling(spss_ctx *ctx, int tile_cells)
+{
+  FastPath *f = ctx->fast;
+  if (f->kind == KIND_ALL_PAIRS) return SPSS_OK;
+  f->tile_cells = tile_cells;
+  int ntiles = 0;
+  std::vector<int> tile_sys;
+  for (int r = 0; r < f->nsys; ++r)
+  {
+    SysParams &S = f->h_sys[r];
+    S.tile0 = ntiles;
+    S.ntiles = S.nc * tiles_per_row(S.nc, tile_cells);
+    ntiles += S.ntiles;
+    tile_sys.insert(tile_sys.end(), (size_t) S.ntiles, r);
+  }
+  f->ntiles = ntiles;
+  SPSS_TRY(f->tiles.reserve(sizeof(TileLayout) * (size_t) ntiles));
+  SPSS_TRY(f->tile_sys.reserve((size_t) ntiles));
+  SPSS_CUDA_TRY(cudaMemcpyAsync(f->tile_sys.ptr, tile_sys.data(), sizeof(int) * ntiles, cudaMemcpyHostToDevice,
+                                ctx->stream));
+  SPSS_CUDA_TRY(cudaMemcpyAsync(f->sys.ptr, f->h_sys.data(), sizeof(SysParams) * f->nsys, cudaMemcpyHostToDevice,
+                                ctx->stream));
+  if (f->kind == KIND_VERLET)
+  {
+    SPSS_TRY(f->vl.reserve((size_t) f->cap * ((size_t) ctx->p.n + 16 * (size_t) ntiles + 16)));
+    SPSS_TRY(f->tile_maxcnt.reserve((size_t) ntiles));
+  }
+  SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  // lists and layouts follow the tiles: rebuild before the next step
+  f->h_ctrl->rebuild = 1;
+  ctx->should_update_lists = 1;
+  SPSS_CUDA_TRY(cudaMemcpyAsync(&f->ctrl->rebuild, &f->h_ctrl->rebuild, sizeof(int), cudaMemcpyHostToDevice,
+                                ctx->stream));
+  for (auto &g : f->graphs)
+  {
+    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+    if (g.second.graph) cudaGraphDestroy(g.second.graph);
+  }
+  f->graphs.clear();
+  SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SPSS_OK;
 }
 
 int fast_create(spss_ctx *ctx)
@@ -1143,30 +1615,54 @@ int fast_create(spss_ctx *ctx)
   ctx->fast = f;
   const spss_params &p = ctx->p;
   const int n = p.n;
-  const int variant = variant_for(ctx, p.variant);
-  switch (variant)
+  std::vector<spss_params> systems = ctx->systems;
+  if (systems.empty()) systems.push_back(p);
+  f->nsys = (int) systems.size();
+  int kind = -1;
+  double lam_max = 0.0;
+  int first = 0, cell0 = 0;
+  for (int r = 0; r < f->nsys; ++r)
   {
-    case SPSS_VARIANT_ALL_PAIRS:
-      f->kind = KIND_ALL_PAIRS;
-      f->nc_build = 1;
-      break;
-    case SPSS_VARIANT_LINKED_LIST:
-      f->kind = KIND_CELLS;
-      f->nc_build = ctx->nc;
-      break;
-    case SPSS_VARIANT_VERLET:
-      // O(N^2) list build = every pair within r_max: cells no smaller than r_max
-      f->kind = KIND_VERLET;
-      f->nc_build = std::max(1, (int) (1.0 / ctx->r_max));
-      if (f->nc_build < 3) return SPSS_ERR_NOT_SUPPORTED;
-      break;
-    case SPSS_VARIANT_LINKED_LIST_VERLET:
-      f->kind = KIND_VERLET;
-      f->nc_build = ctx->nc_verlet;
-      break;
-    default:
-      return SPSS_ERR_NOT_SUPPORTED;  // global field: FP64 contexts
+    const spss_params &q = systems[r];
+    double r_min, r_max;
+    int nc, nc_verlet;
+    derive_lists(q, r_min, r_max, nc, nc_verlet);
+    int k, grid;
+    switch (variant_for_params(q, q.variant))
+    {
+      case SPSS_VARIANT_ALL_PAIRS:
+        k = KIND_ALL_PAIRS;
+        grid = 1;
+        break;
+      case SPSS_VARIANT_LINKED_LIST:
+        k = KIND_CELLS;
+        grid = nc;
+        break;
+      case SPSS_VARIANT_VERLET:
+        // O(N^2) list build = every pair within r_max: cells no smaller than r_max
+        k = KIND_VERLET;
+        grid = std::max(1, (int) (1.0 / r_max));
+        if (grid < 3) return SPSS_ERR_NOT_SUPPORTED;
+        break;
+      case SPSS_VARIANT_LINKED_LIST_VERLET:
+        k = KIND_VERLET;
+        grid = nc_verlet;
+        break;
+      default:
+        return SPSS_ERR_NOT_SUPPORTED;  // global field: FP64 contexts
+    }
+    if (kind >= 0 && k != kind) return SPSS_ERR_NOT_SUPPORTED;  // one list kind per context
+    kind = k;
+    if ((long) cell0 + (long) grid * grid > 0x7fffffffL) return SPSS_ERR_SIZE;
+    f->h_sys.push_back(system_params(q, r, first, grid, cell0, 0, 0, r_min, r_max));
+    first += q.n;
+    cell0 += grid * grid;
+    lam_max = std::max(lam_max, M_PI * r_max * r_max * q.n);
   }
+  if (first != n) return SPSS_ERR_INVALID_ARGUMENT;
+  f->kind = kind;
+  f->total_cells = cell0;
+  f->nc_build = f->h_sys[0].nc;
   if (f->kind == KIND_VERLET) ctx->uses_verlet_list = 1;
   for (int b = 0; b < 2; ++b)
   {
@@ -1185,17 +1681,33 @@ int fast_create(spss_ctx *ctx)
   SPSS_TRY(f->cell_of.reserve(n));
   SPSS_TRY(f->cell_sorted.reserve(n));
   SPSS_TRY(f->vl_cnt.reserve(n));
-  if (f->kind != KIND_ALL_PAIRS)
-    SPSS_TRY(f->tiles.reserve(sizeof(TileLayout) * (size_t) f->nc_build * tiles_per_row(f->nc_build)));
+  SPSS_TRY(f->sys.reserve((size_t) f->nsys));
+  SPSS_TRY(f->sysctl.reserve((size_t) f->nsys));
+  SPSS_TRY(f->sys_of.reserve((size_t) n));
+  {
+    int max_n = 1;
+    for (const SysParams &S : f->h_sys) max_n = std::max(max_n, S.n);
+    f->order_chunks = (max_n + kOrderChunk - 1) / kOrderChunk;
+    SPSS_TRY(f->order_partial.reserve((size_t) f->nsys * f->order_chunks));
+    SPSS_TRY(f->order_out.reserve((size_t) f->nsys * 4));
+    SPSS_TRY(f->stats.reserve((size_t) f->nsys * 5));
+    SPSS_CUDA_TRY(cudaMemsetAsync(f->stats.ptr, 0, sizeof(double) * 5 * f->nsys, ctx->stream));
+  }
   if (f->kind == KIND_VERLET)
   {
     // mean list length: pi r_max^2 n (unit box); room for six standard deviations
-    const double lam = M_PI * ctx->r_max * ctx->r_max * n;
-    f->cap = std::max(16, ((int) std::ceil(lam + 6.0 * std::sqrt(lam) + 8.0) + 3) & ~3);
-    const long ntiles = (long) f->nc_build * tiles_per_row(f->nc_build);
-    SPSS_TRY(f->vl.reserve((size_t) f->cap * ((size_t) n + 16 * (size_t) ntiles + 16)));
-    SPSS_TRY(f->tile_maxcnt.reserve((size_t) ntiles));
+    f->cap = std::max(16, ((int) std::ceil(lam_max + 6.0 * std::sqrt(lam_max) + 8.0) + 3) & ~3);
   }
+  {
+    std::vector<int> sys_of((size_t) n);
+    for (int r = 0; r < f->nsys; ++r)
+      std::fill(sys_of.begin() + f->h_sys[r].first, sys_of.begin() + f->h_sys[r].first + f->h_sys[r].n, r);
+    SPSS_CUDA_TRY(cudaMemcpyAsync(f->sys_of.ptr, sys_of.data(), sizeof(int) * n, cudaMemcpyHostToDevice, ctx->stream));
+    SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  }
+  SPSS_CUDA_TRY(cudaMemsetAsync(f->sysctl.ptr, 0, sizeof(SysControl) * f->nsys, ctx->stream));
+  SPSS_CUDA_TRY(cudaMemcpyAsync(f->sys.ptr, f->h_sys.data(), sizeof(SysParams) * f->nsys, cudaMemcpyHostToDevice,
+                                ctx->stream));
   SPSS_CUDA_TRY(cudaMalloc((void **) &f->ctrl, sizeof(FastControl)));
   SPSS_CUDA_TRY(cudaMallocHost((void **) &f->h_ctrl, sizeof(FastControl)));
   std::memset(f->h_ctrl, 0, sizeof(FastControl));
@@ -1203,6 +1715,16 @@ int fast_create(spss_ctx *ctx)
   f->h_ctrl->uses_verlet = f->kind == KIND_VERLET;
   SPSS_CUDA_TRY(cudaMemcpyAsync(f->ctrl, f->h_ctrl, sizeof(FastControl), cudaMemcpyHostToDevice, ctx->stream));
   SPSS_CUDA_TRY(cudaMemsetAsync(f->vel.ptr, 0, sizeof(float2) * n, ctx->stream));
+  SPSS_TRY(set_tiling(ctx, kTileCellsDefault));
+  // resident CTAs of the persistent tile kernel: one wave
+  {
+    int dev = 0, sms = 0, per_sm = 0;
+    SPSS_CUDA_TRY(cudaGetDevice(&dev));
+    SPSS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    SPSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fast_tile_persistent_kernel<2, 2, KIND_VERLET, true>,
+                                                                kTileThreads, 0));
+    f->persistent_grid = std::max(1, sms * std::max(1, per_sm));
+  }
   SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return SPSS_OK;
 }
@@ -1236,6 +1758,14 @@ void fast_destroy(spss_ctx *ctx)
   f->vl_cnt.release();
   f->tile_maxcnt.release();
   f->tiles.release();
+  f->sys.release();
+  f->sys_of.release();
+  f->tile_sys.release();
+  f->sysctl.release();
+  f->order_partial.release();
+  f->order_out.release();
+  f->stats.release();
+  f->snap.release();
   f->binner.release();
   if (f->ctrl) cudaFree(f->ctrl);
   if (f->h_ctrl) cudaFreeHost(f->h_ctrl);
@@ -1254,7 +1784,7 @@ static int launch_rebuild(spss_ctx *ctx, const FastParams &P)
     fast_cells_kernel<<<blocks_for(n, kTB), kTB, 0, ctx->stream>>>(P, B);
     ++ctx->launches;
     SPSS_TRY(check_launch("fast_cells_kernel"));
-    SPSS_TRY(f->binner.run(f->cell_of.ptr, n, P.nc * P.nc, ctx->stream, ctx->launches));
+    SPSS_TRY(f->binner.run(f->cell_of.ptr, n, f->total_cells, ctx->stream, ctx->launches));
     const FastBuffers B2 = buffers(ctx);  // binner buffers exist now
     fast_permute_kernel<<<blocks_for(n, kTB), kTB, 0, ctx->stream>>>(P, B2);
     ++ctx->launches;
@@ -1268,8 +1798,7 @@ static int launch_rebuild(spss_ctx *ctx, const FastParams &P)
   SPSS_TRY(check_launch("fast_after_rebuild_kernel"));
   if (f->kind != KIND_ALL_PAIRS)
   {
-    const int ntiles = P.nc * tiles_per_row(P.nc);
-    fast_tile_layout_kernel<<<blocks_for(ntiles, 128), 128, 0, ctx->stream>>>(P, buffers(ctx));
+    fast_tile_layout_kernel<<<blocks_for(f->ntiles, 128), 128, 0, ctx->stream>>>(P, buffers(ctx));
     ++ctx->launches;
     SPSS_TRY(check_launch("fast_tile_layout_kernel"));
   }
@@ -1283,18 +1812,37 @@ static int launch_rebuild(spss_ctx *ctx, const FastParams &P)
   return SPSS_OK;
 }
 
+template<int MODEL, int STEPPER, int KIND>
+static void launch_tiles(spss_ctx *ctx, const FastParams &P, const FastBuffers &B, int grid)
+{
+  if (P.persistent)
+  {
+    if (P.nsys > 1)
+      fast_tile_persistent_kernel<MODEL, STEPPER, KIND, true><<<grid, kTileThreads, 0, ctx->stream>>>(P, B);
+    else
+      fast_tile_persistent_kernel<MODEL, STEPPER, KIND, false><<<grid, kTileThreads, 0, ctx->stream>>>(P, B);
+  } else
+  {
+    if (P.nsys > 1) fast_tile_kernel<MODEL, STEPPER, KIND, true><<<grid, kTileThreads, 0, ctx->stream>>>(P, B);
+    else fast_tile_kernel<MODEL, STEPPER, KIND, false><<<grid, kTileThreads, 0, ctx->stream>>>(P, B);
+  }
+}
+
 template<int MODEL, int STEPPER>
 static void launch_step_kind(spss_ctx *ctx, const FastParams &P, const FastBuffers &B)
 {
   const int grid = blocks_for(P.n, kTB);
-  const int tiles = P.nc * tiles_per_row(P.nc);
-  switch (ctx->fast->kind)
+  const int tiles = P.persistent ? std::min(P.ntiles, ctx->fast->persistent_grid) : P.ntiles;
+  if (ctx->fast->kind == KIND_ALL_PAIRS)
   {
-    case KIND_ALL_PAIRS: fast_step_kernel<MODEL, STEPPER, KIND_ALL_PAIRS><<<grid, kTB, 0, ctx->stream>>>(P, B); break;
-    case KIND_CELLS:
-      fast_tile_kernel<MODEL, STEPPER, KIND_CELLS><<<tiles, kTileThreads, 0, ctx->stream>>>(P, B);
-      break;
-    default: fast_tile_kernel<MODEL, STEPPER, KIND_VERLET><<<tiles, kTileThreads, 0, ctx->stream>>>(P, B); break;
+    if (P.nsys > 1) fast_step_kernel<MODEL, STEPPER, KIND_ALL_PAIRS, true><<<grid, kTB, 0, ctx->stream>>>(P, B);
+    else fast_step_kernel<MODEL, STEPPER, KIND_ALL_PAIRS, false><<<grid, kTB, 0, ctx->stream>>>(P, B);
+  } else if (ctx->fast->kind == KIND_CELLS)
+  {
+    launch_tiles<MODEL, STEPPER, KIND_CELLS>(ctx, P, B, tiles);
+  } else
+  {
+    launch_tiles<MODEL, STEPPER, KIND_VERLET>(ctx, P, B, tiles);
   }
 }
 
@@ -1314,10 +1862,27 @@ static int launch_step(spss_ctx *ctx, int stepper, const FastParams &P)
   ++ctx->launches;
   SPSS_TRY(check_launch("fast_step_kernel"));
   if (ctx->timing) SPSS_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
-  fast_control_kernel<<<1, 1, 0, ctx->stream>>>(ctx->fast->ctrl, P.half_skin, P.always_rebuild,
-                                                 ctx->fast->kind == KIND_VERLET);
+  FastPath *f = ctx->fast;
+  fast_control_kernel<<<1, 256, 0, ctx->stream>>>(f->ctrl, f->sysctl.ptr, f->sys.ptr, f->nsys, P.always_rebuild,
+                                                   f->kind == KIND_VERLET);
   ++ctx->launches;
   return check_launch("fast_control_kernel");
+}
+
+// Order parameters of every system; `gated`: only after a sampling step, and
+// then also added to the running averages.
+static int launch_sampling(spss_ctx *ctx, const FastParams &P, int gated)
+{
+  FastPath *f = ctx->fast;
+  const FastBuffers B = buffers(ctx);
+  fast_order_partials_kernel<<<dim3(f->order_chunks, f->nsys), 256, 0, ctx->stream>>>(P, B, f->order_partial.ptr,
+                                                                                        f->order_chunks, gated);
+  ++ctx->launches;
+  SPSS_TRY(check_launch("fast_order_partials_kernel"));
+  fast_order_finish_kernel<<<blocks_for(f->nsys, 128), 128, 0, ctx->stream>>>(
+      P, B, f->order_partial.ptr, f->order_chunks, f->order_out.ptr, f->stats.ptr, gated);
+  ++ctx->launches;
+  return check_launch("fast_order_finish_kernel");
 }
 
 static int sync_control(spss_ctx *ctx)
@@ -1385,11 +1950,12 @@ int fast_step(spss_ctx *ctx, int stepper, double t, double dt)
   return rc;
 }
 
-static int build_graph_on(spss_ctx *ctx, int stepper, const FastParams &P, GraphEntry &g,
+static int build_graph_on(spss_ctx *ctx, int stepper, const FastParams &P, int sampling, GraphEntry &g,
                           unsigned long long launches0);
 
-// One step as a graph: rebuild under a conditional node, then step + control.
-static int build_graph(spss_ctx *ctx, int stepper, double dt, GraphEntry &g)
+// One step as a graph: rebuild under a conditional node, then step + control
+// (+ the gated order-parameter sample).
+static int build_graph(spss_ctx *ctx, int stepper, double dt, int sampling, GraphEntry &g)
 {
   const FastParams P = params(ctx, dt);
   const unsigned long long launches0 = ctx->launches;
@@ -1397,13 +1963,13 @@ static int build_graph(spss_ctx *ctx, int stepper, double dt, GraphEntry &g)
   cudaStream_t work = ctx->stream;
   ctx->timing = 0;
   ctx->stream = ctx->own_stream;  // capture needs a non-legacy stream
-  int rc_all = build_graph_on(ctx, stepper, P, g, launches0);
+  int rc_all = build_graph_on(ctx, stepper, P, sampling, g, launches0);
   ctx->stream = work;
   ctx->timing = timing;
   return rc_all;
 }
 
-static int build_graph_on(spss_ctx *ctx, int stepper, const FastParams &P, GraphEntry &g,
+static int build_graph_on(spss_ctx *ctx, int stepper, const FastParams &P, int sampling, GraphEntry &g,
                           unsigned long long launches0)
 {
   FastPath *f = ctx->fast;
@@ -1443,6 +2009,7 @@ static int build_graph_on(spss_ctx *ctx, int stepper, const FastParams &P, Graph
   // nodes 3-4: step and control
   SPSS_CUDA_TRY(cudaStreamBeginCaptureToGraph(ctx->stream, graph, &cond_node, nullptr, 1, cudaStreamCaptureModeRelaxed));
   rc = launch_step(ctx, stepper, P);
+  if (rc == SPSS_OK && sampling) rc = launch_sampling(ctx, P, 1);
   e = cudaStreamEndCapture(ctx->stream, &graph);
   if (rc != SPSS_OK) return rc;
   SPSS_CUDA_TRY(e);
@@ -1453,40 +2020,247 @@ static int build_graph_on(spss_ctx *ctx, int stepper, const FastParams &P, Graph
   return SPSS_OK;
 }
 
-int fast_steps(spss_ctx *ctx, int stepper, double t0, double dt, int nsteps)
+// nsteps steps: one graph launch each (the first step of a context runs
+// eagerly so that every lazily sized buffer exists before capture).
+static int run_steps(spss_ctx *ctx, int stepper, double dt, long nsteps, int sampling)
 {
-  (void) t0;
   FastPath *f = ctx->fast;
   if (!f->have_state) return SPSS_ERR_INVALID_ARGUMENT;
   if (stepper == SPSS_STEPPER_RK4) return SPSS_ERR_NOT_SUPPORTED;
-  if (nsteps == 0) return SPSS_OK;
+  if (nsteps <= 0) return nsteps == 0 ? SPSS_OK : SPSS_ERR_INVALID_ARGUMENT;
   if (ctx->timing)
   {
-    for (int k = 0; k < nsteps; ++k) SPSS_TRY(fast_step(ctx, stepper, t0 + (k + 1) * dt, dt));
-    return SPSS_OK;
+    for (long k = 0; k < nsteps; ++k)
+    {
+      SPSS_TRY(fast_step(ctx, stepper, 0.0, dt));
+      if (sampling) SPSS_TRY(launch_sampling(ctx, params(ctx, dt), 1));
+    }
+    return sampling ? sync_control(ctx) : SPSS_OK;
   }
   SPSS_TRY(push_host_control(ctx));
-  // the first step runs eagerly so every lazily sized buffer exists before capture
   if (!f->binner.offsets.ptr && f->kind != KIND_ALL_PAIRS)
   {
-    SPSS_TRY(fast_step(ctx, stepper, t0 + dt, dt));
+    SPSS_TRY(fast_step(ctx, stepper, 0.0, dt));
+    if (sampling) SPSS_TRY(launch_sampling(ctx, params(ctx, dt), 1));
     --nsteps;
-    if (nsteps == 0) return SPSS_OK;
+    if (nsteps == 0) return sync_control(ctx);
   }
-  auto key = std::make_pair(stepper, dt);
+  auto key = std::make_tuple(stepper, dt, sampling ? 1 : 0);
   auto it = f->graphs.find(key);
   if (it == f->graphs.end())
   {
     GraphEntry g;
-    SPSS_TRY(build_graph(ctx, stepper, dt, g));
+    SPSS_TRY(build_graph(ctx, stepper, dt, sampling, g));
     it = f->graphs.emplace(key, g).first;
   }
   const int rebuilds0 = f->h_ctrl->rebuilds;
-  for (int k = 0; k < nsteps; ++k) SPSS_CUDA_TRY(cudaGraphLaunch(it->second.exec, ctx->stream));
+  for (long k = 0; k < nsteps; ++k) SPSS_CUDA_TRY(cudaGraphLaunch(it->second.exec, ctx->stream));
   const int rc = sync_control(ctx);
   ctx->launches += (unsigned long long) nsteps * it->second.per_step
       + (unsigned long long) (f->h_ctrl->rebuilds - rebuilds0) * it->second.per_rebuild;
   return rc;
+}
+
+int fast_steps(spss_ctx *ctx, int stepper, double t0, double dt, int nsteps)
+{
+  (void) t0;
+  return run_steps(ctx, stepper, dt, nsteps, 0);
+}
+
+int fast_batch_run(spss_ctx *ctx, int stepper, double dt, long nsteps, long sample_every, long sample_from)
+{
+  FastPath *f = ctx->fast;
+  if (sample_every < 0 || sample_from < 0) return SPSS_ERR_INVALID_ARGUMENT;
+  f->h_ctrl->sample_every = sample_every;
+  f->h_ctrl->sample_from = sample_from;
+  SPSS_CUDA_TRY(cudaMemcpyAsync(&f->ctrl->sample_every, &f->h_ctrl->sample_every, 2 * sizeof(long long),
+                                cudaMemcpyHostToDevice, ctx->stream));
+  return run_steps(ctx, stepper, dt, nsteps, sample_every > 0 ? 1 : 0);
+}
+
+int fast_batch_stats(spss_ctx *ctx, double *h_out)
+{
+  FastPath *f = ctx->fast;
+  std::vector<double> raw((size_t) 5 * f->nsys);
+  SPSS_CUDA_TRY(cudaMemcpyAsync(raw.data(), f->stats.ptr, sizeof(double) * raw.size(), cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  for (int r = 0; r < f->nsys; ++r)
+  {
+    const double *st = &raw[5 * (size_t) r];
+    const double c = st[4];
+    double *o = h_out + 5 * (size_t) r;
+    const double m0 = c > 0 ? st[0] / c : 0.0, m2 = c > 0 ? st[2] / c : 0.0;
+    o[0] = m0;
+    o[1] = c > 0 ? std::max(0.0, st[1] / c - m0 * m0) : 0.0;
+    o[2] = m2;
+    o[3] = c > 0 ? std::max(0.0, st[3] / c - m2 * m2) : 0.0;
+    o[4] = c;
+  }
+  return SPSS_OK;
+}
+
+int fast_batch_reset_stats(spss_ctx *ctx)
+{
+  FastPath *f = ctx->fast;
+  SPSS_CUDA_TRY(cudaMemsetAsync(f->stats.ptr, 0, sizeof(double) * 5 * f->nsys, ctx->stream));
+  SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SPSS_OK;
+}
+
+int fast_system_order_parameters(spss_ctx *ctx, double *h_out)
+{
+  FastPath *f = ctx->fast;
+  if (!f->have_state) return SPSS_ERR_INVALID_ARGUMENT;
+  SPSS_TRY(launch_sampling(ctx, params(ctx, 0.0), 0));
+  SPSS_CUDA_TRY(cudaMemcpyAsync(h_out, f->order_out.ptr, sizeof(double) * 4 * f->nsys, cudaMemcpyDeviceToHost,
+                                ctx->stream));
+  SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SPSS_OK;
+}
+
+int fast_num_systems(const spss_ctx *ctx)
+{
+  return ctx->fast ? ctx->fast->nsys : 1;
+}
+
+int fast_system_first(const spss_ctx *ctx, int r)
+{
+  return ctx->fast->h_sys[r].first;
+}
+
+int fast_set_tiling(spss_ctx *ctx, int tile_cells, int persistent)
+{
+  if (tile_cells < 1 || tile_cells > 4096 || (persistent != 0 && persistent != 1)) return SPSS_ERR_INVALID_ARGUMENT;
+  FastPath *f = ctx->fast;
+  f->persistent = persistent;
+  return set_tiling(ctx, tile_cells);
+}
+
+int fast_get_tiling(spss_ctx *ctx, int *tile_cells, int *persistent)
+{
+  *tile_cells = ctx->fast->tile_cells;
+  *persistent = ctx->fast->persistent;
+  return SPSS_OK;
+}
+
+template<class T>
+static int copy_device(DeviceArray<T> &dst, const T *src, size_t count, cudaStream_t stream)
+{
+  SPSS_TRY(dst.reserve(count));
+  SPSS_CUDA_TRY(cudaMemcpyAsync(dst.ptr, src, sizeof(T) * count, cudaMemcpyDeviceToDevice, stream));
+  return SPSS_OK;
+}
+
+template<class T>
+static int restore_device(T *dst, const DeviceArray<T> &src, size_t count, cudaStream_t stream)
+{
+  SPSS_CUDA_TRY(cudaMemcpyAsync(dst, src.ptr, sizeof(T) * count, cudaMemcpyDeviceToDevice, stream));
+  return SPSS_OK;
+}
+
+static int take_snapshot(spss_ctx *ctx)
+{
+  FastPath *f = ctx->fast;
+  Snapshot &S = f->snap;
+  const size_t n = (size_t) ctx->p.n;
+  cudaStream_t st = ctx->stream;
+  for (int b = 0; b < 2; ++b)
+  {
+    SPSS_TRY(copy_device(S.rec[b], f->rec[b].ptr, n, st));
+    SPSS_TRY(copy_device(S.aux[b], f->aux[b].ptr, n, st));
+  }
+  SPSS_TRY(copy_device(S.vel, f->vel.ptr, n, st));
+  SPSS_TRY(copy_device(S.pid, f->pid.ptr, n, st));
+  SPSS_TRY(copy_device(S.inv, f->inv.ptr, n, st));
+  SPSS_TRY(copy_device(S.img, f->img.ptr, n, st));
+  SPSS_TRY(copy_device(S.turns, f->turns.ptr, n, st));
+  SPSS_TRY(copy_device(S.sysctl, f->sysctl.ptr, (size_t) f->nsys, st));
+  SPSS_TRY(copy_device(S.ctrl, f->ctrl, 1, st));
+  SPSS_CUDA_TRY(cudaStreamSynchronize(st));
+  return SPSS_OK;
+}
+
+// Back to the snapshot; the lists are rebuilt before the next step.
+static int restore_snapshot(spss_ctx *ctx)
+{
+  FastPath *f = ctx->fast;
+  Snapshot &S = f->snap;
+  const size_t n = (size_t) ctx->p.n;
+  cudaStream_t st = ctx->stream;
+  for (int b = 0; b < 2; ++b)
+  {
+    SPSS_TRY(restore_device(f->rec[b].ptr, S.rec[b], n, st));
+    SPSS_TRY(restore_device(f->aux[b].ptr, S.aux[b], n, st));
+  }
+  SPSS_TRY(restore_device(f->vel.ptr, S.vel, n, st));
+  SPSS_TRY(restore_device(f->pid.ptr, S.pid, n, st));
+  SPSS_TRY(restore_device(f->inv.ptr, S.inv, n, st));
+  SPSS_TRY(restore_device(f->img.ptr, S.img, n, st));
+  SPSS_TRY(restore_device(f->turns.ptr, S.turns, n, st));
+  SPSS_TRY(restore_device(f->sysctl.ptr, S.sysctl, (size_t) f->nsys, st));
+  SPSS_CUDA_TRY(cudaMemcpyAsync(f->h_ctrl, S.ctrl.ptr, sizeof(FastControl), cudaMemcpyDeviceToHost, st));
+  SPSS_CUDA_TRY(cudaStreamSynchronize(st));
+  f->h_ctrl->rebuild = 1;
+  SPSS_CUDA_TRY(cudaMemcpyAsync(f->ctrl, f->h_ctrl, sizeof(FastControl), cudaMemcpyHostToDevice, st));
+  SPSS_CUDA_TRY(cudaStreamSynchronize(st));
+  ctx->step_counter = f->h_ctrl->step;
+  ctx->accumulated_displacement = f->h_ctrl->acc;
+  ctx->should_update_lists = 1;
+  S.release();
+  return SPSS_OK;
+}
+
+// Times `steps` steps (graph launches, CUDA events) for every tile width and
+// launch form, keeps the fastest and puts the state back as it was.  The
+// step results do not depend on the tiling.
+int fast_autotune(spss_ctx *ctx, int stepper, double dt, int steps, double *best_ms)
+{
+  FastPath *f = ctx->fast;
+  if (!f->have_state || steps < 1) return SPSS_ERR_INVALID_ARGUMENT;
+  if (stepper == SPSS_STEPPER_RK4) return SPSS_ERR_NOT_SUPPORTED;
+  if (f->kind == KIND_ALL_PAIRS)
+  {
+    if (best_ms) *best_ms = 0.0;
+    return SPSS_OK;
+  }
+  const int timing = ctx->timing;
+  ctx->timing = 0;
+  SPSS_TRY(take_snapshot(ctx));
+  const int widths[] = {8, 16, 32, 64};
+  double best = 1e300;
+  int best_w = f->tile_cells, best_p = f->persistent;
+  int rc = SPSS_OK;
+  for (int w : widths)
+    for (int pers = 0; pers <= 1 && rc == SPSS_OK; ++pers)
+    {
+      f->persistent = pers;
+      rc = set_tiling(ctx, w);
+      if (rc == SPSS_OK) rc = run_steps(ctx, stepper, dt, 2, 0);  // builds the graph, warms up
+      if (rc != SPSS_OK) break;
+      cudaEventRecord(ctx->ev0, ctx->stream);
+      rc = run_steps(ctx, stepper, dt, steps, 0);
+      cudaEventRecord(ctx->ev1, ctx->stream);
+      if (rc != SPSS_OK) break;
+      float ms = 0.0f;
+      SPSS_CUDA_TRY(cudaEventSynchronize(ctx->ev1));
+      SPSS_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+      if (ms / steps < best)
+      {
+        best = ms / steps;
+        best_w = w;
+        best_p = pers;
+      }
+    }
+  f->persistent = best_p;
+  const int rc2 = set_tiling(ctx, best_w);
+  const int rc3 = restore_snapshot(ctx);
+  ctx->timing = timing;
+  if (rc != SPSS_OK) return rc;
+  if (rc2 != SPSS_OK) return rc2;
+  if (rc3 != SPSS_OK) return rc3;
+  if (best_ms) *best_ms = best;
+  return SPSS_OK;
 }
 
 int fast_noise(spss_ctx *ctx, int stepper, unsigned long long step, double *d_out)
@@ -1497,7 +2271,8 @@ int fast_noise(spss_ctx *ctx, int stepper, unsigned long long step, double *d_ou
   nk.seed = ctx->p.seed;
   nk.replica = ctx->p.replica;
   nk.step = step;
-  fast_noise_kernel<<<blocks_for(ctx->p.n, kTB), kTB, 0, ctx->stream>>>(d_out, ctx->p.n, per, nk);
+  fast_noise_kernel<<<blocks_for(ctx->p.n, kTB), kTB, 0, ctx->stream>>>(d_out, ctx->p.n, per, nk, ctx->fast->sys.ptr,
+                                                                       ctx->fast->sys_of.ptr);
   ++ctx->launches;
   return check_launch("fast_noise_kernel");
 }

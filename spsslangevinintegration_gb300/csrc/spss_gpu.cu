@@ -16,9 +16,22 @@ const char *last_error_text();
 // (ParticleSystemFirstOrder.cpp:96-111, ParticleSystemSecondOrder.cpp:91-98)
 int variant_for(const spss_ctx *ctx, int variant)
 {
+  return variant_for_params(ctx->p, variant);
+}
+
+void derive_lists(const spss_params &p, double &r_min, double &r_max, int &nc, int &nc_verlet)
+{
+  r_min = p.rho;
+  r_max = p.r_max > 0.0 ? p.r_max : p.rho + 0.05;  // ParticleSystemFirstOrderPtr.cpp:97-98
+  nc = std::max(1, (int) (1.0 / p.rho));           // ParticleSystemFirstOrder.cpp:37-38
+  nc_verlet = p.nc_verlet > 0 ? p.nc_verlet : nc;
+}
+
+int variant_for_params(const spss_params &p, int variant)
+{
   if (variant != SPSS_VARIANT_DISPATCH) return variant;
-  const double rho = ctx->p.rho;
-  if (ctx->p.model == 1)
+  const double rho = p.rho;
+  if (p.model == 1)
   {
     if (rho >= M_SQRT1_2) return SPSS_VARIANT_GLOBAL_FIELD;
     if (rho <= 0.25) return SPSS_VARIANT_LINKED_LIST_VERLET;
@@ -204,10 +217,7 @@ int spss_create(const spss_params *params, spss_ctx **out)
   if (!ctx) return SPSS_ERR_OUT_OF_MEMORY;
   ctx->p = p;
   ctx->s = p.model == 1 ? 4 : 6;
-  ctx->r_min = p.rho;
-  ctx->r_max = p.r_max > 0.0 ? p.r_max : p.rho + 0.05;  // ParticleSystemFirstOrderPtr.cpp:97-98
-  ctx->nc = std::max(1, (int) (1.0 / p.rho));          // ParticleSystemFirstOrder.cpp:37-38
-  ctx->nc_verlet = p.nc_verlet > 0 ? p.nc_verlet : ctx->nc;
+  derive_lists(p, ctx->r_min, ctx->r_max, ctx->nc, ctx->nc_verlet);
   ctx->should_update_lists = 1;
   int rc = SPSS_OK;
   if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess)
@@ -327,6 +337,7 @@ int spss_set_natural_frequencies(spss_ctx *ctx, const double *freqs, long len)
 int spss_calculate_max_displacement(spss_ctx *ctx, const double *td, long len)
 {
   if (!ctx || !td) return SPSS_ERR_INVALID_ARGUMENT;
+  if (!ctx->systems.empty()) return SPSS_ERR_NOT_SUPPORTED;  // one trigger per system: kept on the device
   if (len != state_len(ctx)) return SPSS_ERR_SIZE;
   // max_i (dx^2 + dy^2) in host FP64, exactly as ParticleSystemFirstOrder.cpp:672-684
   double max2 = 0.0;
@@ -632,6 +643,126 @@ int spss_get_timing(spss_ctx *ctx, double *kernel_ms, unsigned long long *timed_
   if (kernel_ms) *kernel_ms = ctx->timing_ms;
   if (timed_launches) *timed_launches = ctx->timing_count;
   return SPSS_OK;
+}
+
+// ------------------------------------------------ batches of independent systems
+
+int spss_batch_create(const spss_params *systems, int nsys, spss_ctx **out)
+{
+  if (!systems || !out || nsys < 1) return SPSS_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (nsys > SPSS_MAX_SYSTEMS) return SPSS_ERR_SIZE;
+  const spss_params &p0 = systems[0];
+  long total = 0;
+  for (int r = 0; r < nsys; ++r)
+  {
+    const spss_params &q = systems[r];
+    if ((q.model != 1 && q.model != 2) || q.n <= 0 || !(q.rho > 0.0) || !std::isfinite(q.rho))
+      return SPSS_ERR_INVALID_ARGUMENT;
+    if (q.model != p0.model || q.flavor != p0.flavor || q.variant != p0.variant || q.precision != p0.precision ||
+        q.seed != p0.seed)
+      return SPSS_ERR_INVALID_ARGUMENT;
+    total += q.n;
+  }
+  if (p0.precision != SPSS_PRECISION_F32) return SPSS_ERR_NOT_SUPPORTED;  // batches run the GB300 path
+  if (total > 0x7fffffffL) return SPSS_ERR_SIZE;
+  spss_ctx *ctx = new (std::nothrow) spss_ctx();
+  if (!ctx) return SPSS_ERR_OUT_OF_MEMORY;
+  ctx->p = p0;
+  ctx->p.n = (int) total;
+  ctx->systems.assign(systems, systems + nsys);
+  ctx->s = p0.model == 1 ? 4 : 6;
+  derive_lists(p0, ctx->r_min, ctx->r_max, ctx->nc, ctx->nc_verlet);
+  ctx->should_update_lists = 1;
+  if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+  {
+    cudaGetLastError();
+    delete ctx;
+    return SPSS_ERR_CUDA;
+  }
+  ctx->stream = ctx->own_stream;
+  if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess)
+  {
+    cudaGetLastError();
+    spss_destroy(ctx);
+    return SPSS_ERR_CUDA;
+  }
+  const int rc = fast_create(ctx);
+  if (rc != SPSS_OK)
+  {
+    spss_destroy(ctx);
+    return rc;
+  }
+  *out = ctx;
+  return SPSS_OK;
+}
+
+int spss_batch_size(spss_ctx *ctx, int *nsys, long *first)
+{
+  if (!ctx) return SPSS_ERR_INVALID_ARGUMENT;
+  const int ns = is_f64(ctx) ? 1 : fast_num_systems(ctx);
+  if (nsys) *nsys = ns;
+  if (first)
+  {
+    for (int r = 0; r < ns; ++r) first[r] = is_f64(ctx) ? 0 : fast_system_first(ctx, r);
+    first[ns] = ctx->p.n;
+  }
+  return SPSS_OK;
+}
+
+int spss_batch_order_parameters(spss_ctx *ctx, double *out, long len)
+{
+  if (!ctx || !out) return SPSS_ERR_INVALID_ARGUMENT;
+  if (is_f64(ctx)) return SPSS_ERR_NOT_SUPPORTED;
+  if (len != 4L * fast_num_systems(ctx)) return SPSS_ERR_SIZE;
+  return fast_system_order_parameters(ctx, out);
+}
+
+int spss_batch_run(spss_ctx *ctx, int stepper, double t0, double dt, long nsteps, long sample_every, long sample_from)
+{
+  (void) t0;
+  if (!ctx || nsteps < 0) return SPSS_ERR_INVALID_ARGUMENT;
+  SPSS_TRY(check_stepper(ctx, stepper));
+  if (is_f64(ctx)) return SPSS_ERR_NOT_SUPPORTED;
+  const int rc = fast_batch_run(ctx, stepper, dt, nsteps, sample_every, sample_from);
+  return rc;
+}
+
+int spss_batch_stats(spss_ctx *ctx, double *out, long len)
+{
+  if (!ctx || !out) return SPSS_ERR_INVALID_ARGUMENT;
+  if (is_f64(ctx)) return SPSS_ERR_NOT_SUPPORTED;
+  if (len != (long) SPSS_STATS_PER_SYSTEM * fast_num_systems(ctx)) return SPSS_ERR_SIZE;
+  return fast_batch_stats(ctx, out);
+}
+
+int spss_batch_reset_stats(spss_ctx *ctx)
+{
+  if (!ctx) return SPSS_ERR_INVALID_ARGUMENT;
+  if (is_f64(ctx)) return SPSS_ERR_NOT_SUPPORTED;
+  return fast_batch_reset_stats(ctx);
+}
+
+int spss_set_tiling(spss_ctx *ctx, int tile_cells, int persistent)
+{
+  if (!ctx) return SPSS_ERR_INVALID_ARGUMENT;
+  if (is_f64(ctx)) return SPSS_ERR_NOT_SUPPORTED;
+  return fast_set_tiling(ctx, tile_cells, persistent);
+}
+
+int spss_get_tiling(spss_ctx *ctx, int *tile_cells, int *persistent)
+{
+  if (!ctx || !tile_cells || !persistent) return SPSS_ERR_INVALID_ARGUMENT;
+  if (is_f64(ctx)) return SPSS_ERR_NOT_SUPPORTED;
+  return fast_get_tiling(ctx, tile_cells, persistent);
+}
+
+int spss_autotune(spss_ctx *ctx, int stepper, double dt, int steps, double *best_ms_per_step)
+{
+  if (!ctx) return SPSS_ERR_INVALID_ARGUMENT;
+  SPSS_TRY(check_stepper(ctx, stepper));
+  if (is_f64(ctx)) return SPSS_ERR_NOT_SUPPORTED;
+  return fast_autotune(ctx, stepper, dt, steps, best_ms_per_step);
 }
 
 }  // extern "C"

@@ -93,15 +93,18 @@ __device__ __forceinline__ void box_muller_f64(uint32_t a, uint32_t b, double &z
 // The angle is uniform on (-pi, pi) and goes through the hardware sine and
 // cosine (absolute error below 2^-21 there); the radius keeps the accurate
 // logarithm so that small normals keep their relative accuracy.
+// Rounding is spelled out (__fmul_rn, __fadd_rn) so every inlined copy of this
+// function produces the same bits.
 __device__ __forceinline__ void box_muller_f32(uint32_t a, uint32_t b, float &z0, float &z1)
 {
-  const float u1 = ((float) (a >> 8) + 0.5f) * 5.9604644775390625e-8f;
-  const float theta = ((float) (b >> 8) * 5.9604644775390625e-8f - 0.49999997f) * 6.2831853f;
-  const float r = sqrtf(-2.0f * logf(u1));
+  const float u1 = __fmul_rn(__fadd_rn((float) (a >> 8), 0.5f), 5.9604644775390625e-8f);
+  const float theta = __fmul_rn(__fadd_rn(__fmul_rn((float) (b >> 8), 5.9604644775390625e-8f), -0.49999997f),
+                                6.2831853f);
+  const float r = sqrtf(__fmul_rn(-2.0f, logf(u1)));
   float s, c;
   __sincosf(theta, &s, &c);
-  z0 = r * c;
-  z1 = r * s;
+  z0 = __fmul_rn(r, c);
+  z1 = __fmul_rn(r, s);
 }
 
 // Normal number d (0-based, reference draw order) of one particle at one step.
@@ -209,7 +212,8 @@ struct FastPath;
 
 struct spss_ctx
 {
-  spss_params p{};
+  spss_params p{};  // a batch: the first system's parameters, n = all particles
+  std::vector<spss_params> systems;  // a batch: every system (empty for one system)
   int s = 4;
   cudaStream_t stream = nullptr;      // where work is issued
   cudaStream_t own_stream = nullptr;  // created with the context; graph capture runs here
@@ -272,8 +276,22 @@ int fast_noise(spss_ctx *ctx, int stepper, unsigned long long step, double *d_ou
 int fast_complementary_force(spss_ctx *ctx, double *d_out);
 int fast_apply_pbc(spss_ctx *ctx);
 
+int fast_set_tiling(spss_ctx *ctx, int tile_cells, int persistent);
+int fast_get_tiling(spss_ctx *ctx, int *tile_cells, int *persistent);
+int fast_autotune(spss_ctx *ctx, int stepper, double dt, int steps, double *best_ms);
+int fast_system_order_parameters(spss_ctx *ctx, double *h_out);
+int fast_batch_run(spss_ctx *ctx, int stepper, double dt, long nsteps, long sample_every, long sample_from);
+int fast_batch_stats(spss_ctx *ctx, double *h_out);
+int fast_batch_reset_stats(spss_ctx *ctx);
+int fast_num_systems(const spss_ctx *ctx);
+int fast_system_first(const spss_ctx *ctx, int r);
+
 // Shared helpers, spss_gpu.cu
 int order_parameters_aos(spss_ctx *ctx, const double *d_aos, double out[4]);
 int host_calculate_max_displacement(spss_ctx *ctx, double max2);
 int variant_for(const spss_ctx *ctx, int variant);
+int variant_for_params(const spss_params &p, int variant);
+// List geometry of a system: r_min = rho, r_max (Verlet cutoff), the cell grid
+// of the linked list and of the Verlet rebuild.
+void derive_lists(const spss_params &p, double &r_min, double &r_max, int &nc, int &nc_verlet);
 }  // namespace spss

@@ -52,3 +52,25 @@ def test_error_strings_without_gpu():
     # argument checks run before any CUDA call
     assert L.spss_create(None, None) == _native.ERR_INVALID_ARGUMENT
     assert L.spss_step(None, 0, 0.0, 0.01) == _native.ERR_INVALID_ARGUMENT
+
+
+def test_batch_argument_checks_without_gpu():
+    """spss_batch_create validates the system table before any CUDA call."""
+    from spsslangevinintegration_gb300 import _native, make_params
+
+    L = _native.lib(built_library())
+    h = ctypes.c_void_p()
+    a = make_params(2, 1000, 0.05, precision=_native.PRECISION_F32, variant=_native.LINKED_LIST, seed=1)
+    b = make_params(1, 500, 0.05, precision=_native.PRECISION_F32, variant=_native.LINKED_LIST, seed=1)
+    arr = (_native.Params * 2)(a, b)
+    assert L.spss_batch_create(arr, 2, ctypes.byref(h)) == _native.ERR_INVALID_ARGUMENT  # models differ
+    c = make_params(2, 1000, 0.05, precision=_native.PRECISION_F32, variant=_native.LINKED_LIST, seed=2)
+    arr = (_native.Params * 2)(a, c)
+    assert L.spss_batch_create(arr, 2, ctypes.byref(h)) == _native.ERR_INVALID_ARGUMENT  # seeds differ
+    d = make_params(2, 1000, 0.05, precision=_native.PRECISION_F64, variant=_native.LINKED_LIST, seed=1)
+    arr = (_native.Params * 1)(d)
+    assert L.spss_batch_create(arr, 1, ctypes.byref(h)) == _native.ERR_NOT_SUPPORTED  # batches run in F32
+    assert L.spss_batch_create(arr, 0, ctypes.byref(h)) == _native.ERR_INVALID_ARGUMENT
+    assert L.spss_batch_run(None, 1, 0.0, 0.005, 10, 1, 0) == _native.ERR_INVALID_ARGUMENT
+    assert L.spss_set_tiling(None, 32, 0) == _native.ERR_INVALID_ARGUMENT
+    assert L.spss_autotune(None, 1, 0.005, 2, None) == _native.ERR_INVALID_ARGUMENT

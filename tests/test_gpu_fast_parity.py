@@ -16,36 +16,11 @@ Tolerances (stated here, checked below):
 import numpy as np
 import pytest
 
-from helpers import gpu_context, min_image, oracle_system
+from helpers import gpu_context, initial, min_image, oracle_system, params
 
 pytestmark = pytest.mark.gpu
 
 F32 = 1
-
-
-def initial(model, n, seed, v=0.01, omega=0.5):
-    rng = np.random.default_rng(seed)
-    s = 4 if model == 1 else 6
-    x = np.zeros((n, s))
-    x[:, 0], x[:, 1] = rng.random(n), rng.random(n)
-    phi = rng.uniform(-np.pi, np.pi, n)
-    if model == 1:
-        x[:, 2], x[:, 3] = phi, rng.uniform(-omega, omega, n)
-    else:
-        x[:, 2], x[:, 3] = v * np.cos(phi), v * np.sin(phi)
-        x[:, 4], x[:, 5] = phi, rng.uniform(-omega, omega, n)
-    return x.reshape(-1)
-
-
-def params(model, n, density=2.0, R=1.0, v0=0.5, m=1.0, D=0.1, sigma=1.0, alpha=0.0):
-    """Physical parameters mapped to the reference's unit box (L = sqrt(N/density))."""
-    L = np.sqrt(n / density)
-    p = dict(model=model, n=n, rho=R / L, flavor="ptr", v0=v0 / L, sigma=sigma / m, alpha=alpha)
-    if model == 1:
-        p.update(xi=0.1, D_phi=D)
-    else:
-        p.update(xi_r=1.0 / m, xi_phi=1.0 / m, D_r=1e-3 / L ** 2, D_phi=D / m ** 2)
-    return p
 
 
 def state_err(got, ref, s):
