@@ -181,6 +181,86 @@ def cpu_baseline(n, budget_s=20.0, bench_lib=True):
                       "step (%.1f s), FP64 oracle port, OpenMP %d threads" % (n, steps, el, cores)}
 
 
+SWEEP_SYSTEMS, SWEEP_STEPS_PER_POINT, SWEEP_SAMPLE_EVERY = 512, 20000, 10
+
+
+def sweep_cpu_sample(points, budget_s=8.0):
+    """The oracle port (FP64, all cores) on the sweep's most common system
+    size: SE steps with cell lists, as particle-steps/s."""
+    from oracle import binding as ob
+    from spsslangevinintegration_gb300 import sweep
+
+    cores = os.cpu_count() or 1
+    ob.set_threads(cores, bench=True)
+    pt = sorted(points, key=lambda q: q["n"])[len(points) // 2]
+    kw = sweep.system_params(pt)
+    sysm = ob.System(2, kw["n"], kw["rho"], v0=kw["v0"], xi_r=kw["xi_r"], D_r=kw["D_r"], xi_phi=kw["xi_phi"],
+                     D_phi=kw["D_phi"], sigma=kw["sigma"], bench=True)
+    x = sweep.initial_state(kw["n"], np.sqrt(kw["n"] / pt["density"]), 0)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        normals = ob.philox_normals(0, steps, 0, 3 * kw["n"], bench=True)
+        sysm.step(ob.SE, 2, x, DT * (steps + 1), DT, normals)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or steps >= 2000:
+            break
+    sysm.close()
+    return kw["n"] * steps / el, cores, "N=%d (median system), %d SE steps with cell lists, FP64 oracle port, " \
+        "OpenMP %d threads, %.1f s" % (kw["n"], steps, cores, el)
+
+
+def run_sweep_leg(args, rank, world, barrier, max_over_ranks):
+    """Batched parameter sweep: 512 independent systems in one batch context
+    (one CUDA graph per step for all systems), tiling picked by the autotuner;
+    phase-diagram points per hour at 20,000 steps per point."""
+    import torch
+
+    from spsslangevinintegration_gb300 import STOCHASTIC_EULER, sweep
+    from spsslangevinintegration_gb300.replicas import shard
+
+    points = sweep.replica_table(SWEEP_SYSTEMS, seed=0)
+    mine = [points[i] for i in shard(len(points), world, rank)]
+    b = sweep.make_batch(mine, seed=0, first_replica=shard(len(points), world, rank)[0])
+    b.steps(STOCHASTIC_EULER, 0.0, DT, 3)
+    tune_ms = b.autotune(STOCHASTIC_EULER, DT, steps=4)
+    b.run(STOCHASTIC_EULER, 0.0, DT, 10, sample_every=SWEEP_SAMPLE_EVERY, sample_from=0)
+    steps = max(20, min(args.sweep_steps, 2000))
+    launches0 = b.kernel_launches
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.run(STOCHASTIC_EULER, 0.0, DT, steps, sample_every=SWEEP_SAMPLE_EVERY, sample_from=0)
+    b.synchronize()
+    barrier()
+    el = max_over_ranks(time.perf_counter() - t0)
+    launches = b.kernel_launches - launches0
+    tiling = b.tiling()
+    total_n = sum(p["n"] for p in points)
+    b.close()
+    if rank != 0:
+        return None
+    s_per_step = el / steps
+    out = {
+        "workload": "%d independent systems (second-order model): N log-uniform in [1024, 65536] (total %d), "
+                    "sigma uniform in [0, 3], D log-uniform in [0.01, 1], m in {0.1, 1, 10}, density 2, R=1, "
+                    "v0=0.5, cell lists rebuilt every step, StochasticEuler dt=0.005, per-system time-averaged "
+                    "phase and velocity order parameters sampled every %d steps" % (len(points), total_n,
+                                                                                   SWEEP_SAMPLE_EVERY),
+        "steps_timed": steps, "ms_per_step": 1e3 * s_per_step, "particle_steps_per_s": total_n / s_per_step,
+        "points_per_hour": len(points) * 3600.0 / (SWEEP_STEPS_PER_POINT * s_per_step),
+        "points_per_hour_unit": "phase-diagram points per hour at %d steps per point" % SWEEP_STEPS_PER_POINT,
+        "tiling": {"tile_cells": tiling[0], "persistent": tiling[1], "autotuned_ms_per_step": tune_ms},
+        "gpu_launches_per_step": launches / steps,
+        "timing": "wall clock around %d steps (graph launches, one host synchronisation), max over ranks" % steps,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        rate, cores, sample = sweep_cpu_sample(points, budget_s=args.cpu_seconds / 2)
+        out["cpu_baseline"] = {"particle_steps_per_s": rate, "cores": cores, "kind": "port", "sample": sample,
+                               "points_per_hour": len(points) * 3600.0 * rate / (total_n * SWEEP_STEPS_PER_POINT)}
+    return out
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -326,6 +406,10 @@ def run_ours(args, rank, world, local_rank):
     }
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(n, budget_s=args.cpu_seconds)
+    if not args.no_sweep:
+        sw = run_sweep_leg(args, rank, world, barrier, max_over_ranks)
+        if sw is not None:
+            line["sweep"] = sw
     print(json.dumps(line), flush=True)
     return 0
 
@@ -339,6 +423,8 @@ def main():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--sweep-steps", type=int, default=400)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

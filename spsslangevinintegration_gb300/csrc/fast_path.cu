@@ -48,7 +48,8 @@ struct FastControl
   unsigned int unused;
   int overflow;             // largest Verlet count seen beyond capacity (0: none)
   int rebuilds;             // number of rebuilds performed
-  int error;                // bit 0: displacement too large for the fixed-point increment; bit 1: staging timeout
+  int error;                // bit 0: displacement too large for the fixed-point increment; bit 1: staging
+                            // timeout; bit 2: stencil cell outside the staged segments
   int uses_verlet;
   int tile_next;            // work counter of the persistent tile kernel
   long long sample_every;   // order-parameter samples after steps that are multiples of this (0: none)
@@ -193,8 +194,11 @@ struct FastPath
   std::map<std::tuple<int, double, int>, GraphEntry> graphs;  // (stepper, dt, with sampling)
   // per-system order parameters and their time averages
   DeviceArray<OrderSums> order_partial;
+  DeviceArray<int2> order_items;   // (system, first slot) of every chunk, systems in order
+  DeviceArray<int> order_first;    // first chunk of every system, nsys + 1 entries
   DeviceArray<double> order_out, stats;
-  int order_chunks = 1;
+  int order_chunks = 1;  // chunks of all systems
+  int order_grid = 1;
   Snapshot snap;
 };
 
@@ -301,6 +305,26 @@ struct Acc
 // image by integer subtraction); inside the guard band the decision is
 // recomputed in FP64 from the full 64-bit positions, so it equals the FP64
 // decision for these positions.
+// The FP64 cutoff decision from the full 64-bit positions, for a pair inside
+// the guard band (a few pairs per step).
+__device__ __forceinline__ bool exact_within_inline(uint32_t xh, uint32_t yh, uint32_t xl, uint32_t yl, uint64_t Xi,
+                                                   uint64_t Yi, double rho2)
+{
+  const double ex = (double) (long long) (join64(xh, xl) - Xi) * 5.421010862427522e-20;
+  const double ey = (double) (long long) (join64(yh, yl) - Yi) * 5.421010862427522e-20;
+  return __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)) <= rho2;
+}
+
+// Out of line, for the stencil scans: keeps their loops small in the
+// instruction cache (the Verlet-list walk keeps the inline form, which costs
+// no call).
+__device__ __noinline__ bool exact_within(uint32_t xh, uint32_t yh, uint32_t xl, uint32_t yl, uint64_t Xi,
+                                          uint64_t Yi, double rho2)
+{
+  return exact_within_inline(xh, yh, xl, yl, Xi, Yi, rho2);
+}
+
+template<bool OUTLINE>
 __device__ __forceinline__ bool in_range(const FastParams &P, const uint4 &ri, uint64_t Xi, uint64_t Yi,
                                          const uint4 &rj, const uint4 *__restrict__ aux, int j)
 {
@@ -311,9 +335,8 @@ __device__ __forceinline__ bool in_range(const FastParams &P, const uint4 &ri, u
   if (fabsf(d2 - P.rho2_f) <= P.band_f)
   {
     const uint2 l = __ldg(reinterpret_cast<const uint2 *>(&aux[j]));
-    const double ex = (double) (long long) (join64(rj.x, l.x) - Xi) * 5.421010862427522e-20;
-    const double ey = (double) (long long) (join64(rj.y, l.y) - Yi) * 5.421010862427522e-20;
-    in = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)) <= P.rho2_d;
+    in = OUTLINE ? exact_within(rj.x, rj.y, l.x, l.y, Xi, Yi, P.rho2_d)
+                 : exact_within_inline(rj.x, rj.y, l.x, l.y, Xi, Yi, P.rho2_d);
   }
   return in;
 }
@@ -328,18 +351,18 @@ __device__ __forceinline__ void accumulate(Acc &a, const uint4 &rj, float wj)
   a.card += 1;
 }
 
-template<bool OMEGA>
+template<bool OMEGA, bool OUTLINE>
 __device__ __forceinline__ void candidate(const FastParams &P, const uint4 &ri, uint64_t Xi, uint64_t Yi,
                                           const uint4 *__restrict__ rec, const uint4 *__restrict__ aux, int j, Acc &a)
 {
   const uint4 rj = __ldg(&rec[j]);
-  if (in_range(P, ri, Xi, Yi, rj, aux, j)) accumulate(a, rj, OMEGA ? __uint_as_float(__ldg(&aux[j].w)) : 0.0f);
+  if (in_range<OUTLINE>(P, ri, Xi, Yi, rj, aux, j)) accumulate(a, rj, OMEGA ? __uint_as_float(__ldg(&aux[j].w)) : 0.0f);
 }
 
 // Four list entries at a time: the entry loads, then the record loads, then
 // the omega loads of the pairs in range are issued together, so a thread has
 // several gathers in flight instead of a chain of dependent ones.
-template<bool OMEGA>
+template<bool OMEGA, bool OUTLINE>
 __device__ __forceinline__ void candidates4(const FastParams &P, const uint4 &ri, uint64_t Xi, uint64_t Yi,
                                             const uint4 *__restrict__ rec, const uint4 *__restrict__ aux,
                                             const int j[4], Acc &a)
@@ -349,7 +372,7 @@ __device__ __forceinline__ void candidates4(const FastParams &P, const uint4 &ri
   for (int u = 0; u < 4; ++u) r[u] = __ldg(&rec[j[u]]);
   bool in[4];
 #pragma unroll
-  for (int u = 0; u < 4; ++u) in[u] = in_range(P, ri, Xi, Yi, r[u], aux, j[u]);
+  for (int u = 0; u < 4; ++u) in[u] = in_range<OUTLINE>(P, ri, Xi, Yi, r[u], aux, j[u]);
   float w[4];
 #pragma unroll
   for (int u = 0; u < 4; ++u) w[u] = (OMEGA && in[u]) ? __uint_as_float(__ldg(&aux[j[u]].w)) : 0.0f;
@@ -543,6 +566,17 @@ struct TileLayout
   int nseg, total;     // staged segments (ascending slot order) and records
   int start[6], len[6], base[6];
   int staged;          // the neighbourhood fits kTileCap records
+  int row, col0, ncols;  // the tile's cells: row `row`, columns col0 .. col0 + ncols - 1
+};
+
+// Cell-list stencil of one cell of a staged tile: for each stencil row (dy =
+// -1, 0, 1) the staged records of the three cells (cx - 1, cx, cx + 1, wrapped)
+// as at most three contiguous runs of staged indices, in the reference's
+// stencil order (ParticleSystemFirstOrder.cpp:47-52).
+constexpr int kRunCells = 64;  // widest tile with a run table
+struct StencilRuns
+{
+  short s[3][3], e[3][3];  // [dy + 1][piece]
 };
 
 __host__ __device__ __forceinline__ int tiles_per_row(int nc, int tc)
@@ -559,6 +593,9 @@ __device__ void tile_layout(int t, int nc, int tc, const int *__restrict__ off, 
   const int cx_lo = bx * tc, cx_hi = min(nc, cx_lo + tc);
   L.p_begin = off[cy * nc + cx_lo];
   L.p_end = off[cy * nc + cx_hi];
+  L.row = cy;
+  L.col0 = cx_lo;
+  L.ncols = cx_hi - cx_lo;
   L.nseg = 0;
   L.total = 0;
   L.staged = 0;
@@ -664,6 +701,58 @@ __device__ __forceinline__ int staged_slot(const TileLayout &L, int idx)
   return 0;
 }
 
+// Run table and per-particle cell column of a staged tile (all threads of the
+// CTA; cell offsets `coff` of the tile's system).  Returns through `self_base`
+// the shift from a slot of the tile to its staged index.
+__device__ __forceinline__ void build_runs(const TileLayout &L, const int *__restrict__ coff, int nc,
+                                           StencilRuns *runs, unsigned char *col_of, int *self_base, int *error)
+{
+  for (int w = threadIdx.x; w < 3 * L.ncols; w += blockDim.x)
+  {
+    const int k = w / 3, dy = w - 3 * k - 1;
+    const int cx = L.col0 + k;
+    const int row = wrap_cell(L.row + dy, nc) * nc;
+    const int cells[3] = {wrap_cell(cx - 1, nc), cx, wrap_cell(cx + 1, nc)};
+    short ps[3] = {0, 0, 0}, pe[3] = {0, 0, 0};
+    int np = 0;
+    for (int u = 0; u < 3; ++u)
+    {
+      const int b = coff[row + cells[u]], e = coff[row + cells[u] + 1];
+      if (e <= b) continue;
+      const int i0 = staged_index(L, b);
+      if (i0 < 0)
+      {
+        atomicOr(error, 4);  // a stencil cell outside the staged segments (the layout rules this out)
+        continue;
+      }
+      if (np > 0 && pe[np - 1] == i0)
+      {
+        pe[np - 1] = (short) (i0 + (e - b));
+      } else
+      {
+        ps[np] = (short) i0;
+        pe[np] = (short) (i0 + (e - b));
+        ++np;
+      }
+    }
+    for (int u = 0; u < 3; ++u)
+    {
+      runs[k].s[dy + 1][u] = ps[u];
+      runs[k].e[dy + 1][u] = pe[u];
+    }
+    if (dy == 0)
+    {
+      const int rb = L.row * nc;
+      for (int q = coff[rb + cx]; q < coff[rb + cx + 1]; ++q) col_of[q - L.p_begin] = (unsigned char) k;
+    }
+  }
+  if (threadIdx.x == 0)
+  {
+    for (int k = 0; k < L.nseg; ++k)
+      if (L.p_begin >= L.start[k] && L.p_begin < L.start[k] + L.len[k]) *self_base = L.base[k] - L.start[k];
+  }
+}
+
 __device__ __forceinline__ uint32_t smem_u32(const void *p)
 {
   return (uint32_t) __cvta_generic_to_shared(p);
@@ -754,13 +843,13 @@ __device__ __forceinline__ void gather_sums(const FastParams &P, const FastBuffe
       {
         const int j[4] = {q + (int) lp[0], q + (int) lp[n], q + (int) lp[2 * n], q + (int) lp[3 * n]};
         lp += 4 * n;
-        candidates4<OMEGA>(P, ri, Xi, Yi, rec, aux, j, a);
+        candidates4<OMEGA, KIND == KIND_CELLS>(P, ri, Xi, Yi, rec, aux, j, a);
       }
       for (; m < cnt; ++m)
       {
         const int j = q + (int) lp[0];
         lp += n;
-        candidate<OMEGA>(P, ri, Xi, Yi, rec, aux, j, a);
+        candidate<OMEGA, KIND == KIND_CELLS>(P, ri, Xi, Yi, rec, aux, j, a);
       }
       return;
     }
@@ -771,7 +860,7 @@ __device__ __forceinline__ void gather_sums(const FastParams &P, const FastBuffe
   {
     const int end = P.first + P.sub_n;
     for (int j = P.first; j < end; ++j)
-      if (j != q) candidate<OMEGA>(P, ri, Xi, Yi, rec, aux, j, a);
+      if (j != q) candidate<OMEGA, KIND == KIND_CELLS>(P, ri, Xi, Yi, rec, aux, j, a);
     return;
   }
   const int *coff = B.cell_off + P.cell0;
@@ -786,14 +875,14 @@ __device__ __forceinline__ void gather_sums(const FastParams &P, const FastBuffe
       const int jc = jy * P.nc + wrap_cell(cx + sx, P.nc);
       const int e = coff[jc + 1];
       for (int j = coff[jc]; j < e; ++j)
-        if (j != q) candidate<OMEGA>(P, ri, Xi, Yi, rec, aux, j, a);
+        if (j != q) candidate<OMEGA, KIND == KIND_CELLS>(P, ri, Xi, Yi, rec, aux, j, a);
     }
   }
 }
 
 // One staged candidate: the record comes from shared memory; the guard band
 // (rare) still reads the slot's low position words from global memory.
-template<bool OMEGA>
+template<bool OMEGA, bool OUTLINE = true>
 __device__ __forceinline__ void candidate_staged(const FastParams &P, const uint4 &ri, uint64_t Xi, uint64_t Yi,
                                                  const uint4 *srec, const uint4 *saux, int idx, Acc &a)
 {
@@ -805,9 +894,8 @@ __device__ __forceinline__ void candidate_staged(const FastParams &P, const uint
   if (fabsf(d2 - P.rho2_f) <= P.band_f)
   {
     const uint4 l = saux[idx];
-    const double ex = (double) (long long) (join64(rj.x, l.x) - Xi) * 5.421010862427522e-20;
-    const double ey = (double) (long long) (join64(rj.y, l.y) - Yi) * 5.421010862427522e-20;
-    in = __dadd_rn(__dmul_rn(ex, ex), __dmul_rn(ey, ey)) <= P.rho2_d;
+    in = OUTLINE ? exact_within(rj.x, rj.y, l.x, l.y, Xi, Yi, P.rho2_d)
+                 : exact_within_inline(rj.x, rj.y, l.x, l.y, Xi, Yi, P.rho2_d);
   }
   if (in) accumulate(a, rj, OMEGA ? __uint_as_float(saux[idx].w) : 0.0f);
 }
@@ -818,8 +906,25 @@ __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const Fa
                                                    const uint4 *saux, const TileLayout &L,
                                                    const uint4 *__restrict__ rec, const uint4 *__restrict__ aux, int q,
                                                    int cnt, const short *lp, int stride, const uint4 &ri, uint64_t Xi,
-                                                   uint64_t Yi, Acc &a)
+                                                   uint64_t Yi, Acc &a, const StencilRuns *runs,
+                                                   const unsigned char *col_of, int self_base)
 {
+  if (KIND == KIND_CELLS && runs)
+  {
+    // cell list from the tile's run table: three rows of contiguous staged records
+    const StencilRuns &R = runs[col_of[q - L.p_begin]];
+    const int self = q + self_base;
+#pragma unroll 1
+    for (int r = 0; r < 3; ++r)
+#pragma unroll 1
+      for (int u = 0; u < 3; ++u)
+      {
+        const int e = R.e[r][u];
+        for (int idx = R.s[r][u]; idx < e; ++idx)
+          if (idx != self) candidate_staged<OMEGA, true>(P, ri, Xi, Yi, srec, saux, idx, a);
+      }
+    return;
+  }
   if (KIND == KIND_VERLET && cnt >= 0)
   {
     const long n = stride;
@@ -828,14 +933,14 @@ __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const Fa
     {
       const int i0 = lp[0], i1 = lp[n], i2 = lp[2 * n], i3 = lp[3 * n];
       lp += 4 * n;
-      candidate_staged<OMEGA>(P, ri, Xi, Yi, srec, saux, i0, a);
-      candidate_staged<OMEGA>(P, ri, Xi, Yi, srec, saux, i1, a);
-      candidate_staged<OMEGA>(P, ri, Xi, Yi, srec, saux, i2, a);
-      candidate_staged<OMEGA>(P, ri, Xi, Yi, srec, saux, i3, a);
+      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, i0, a);
+      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, i1, a);
+      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, i2, a);
+      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, i3, a);
     }
     for (; m < cnt; ++m)
     {
-      candidate_staged<OMEGA>(P, ri, Xi, Yi, srec, saux, lp[0], a);
+      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, lp[0], a);
       lp += n;
     }
     return;
@@ -858,12 +963,12 @@ __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const Fa
       {
         // not inside the staged segments (cannot happen for a cell of this tile's stencil)
         for (int j = b; j < e; ++j)
-          if (j != q) candidate<OMEGA>(P, ri, Xi, Yi, rec, aux, j, a);
+          if (j != q) candidate<OMEGA, KIND == KIND_CELLS>(P, ri, Xi, Yi, rec, aux, j, a);
         continue;
       }
       const int self = q - b;
       for (int u = 0; u < e - b; ++u)
-        if (u != self) candidate_staged<OMEGA>(P, ri, Xi, Yi, srec, saux, i0 + u, a);
+        if (u != self) candidate_staged<OMEGA, KIND == KIND_CELLS>(P, ri, Xi, Yi, srec, saux, i0 + u, a);
     }
   }
 }
@@ -1064,7 +1169,8 @@ template<int MODEL, int STEPPER, int KIND>
 __device__ __forceinline__ void step_tile(const FastParams &Q, const FastBuffers &B, const TileLayout &L,
                                           const uint4 *srec, const uint4 *saux, const short *slist, const short *glist,
                                           int list_staged, int list_stride, bool staged, const uint4 *rin,
-                                          const uint4 *ain, uint4 *rout, uint4 *aout, float &d2max, int &err)
+                                          const uint4 *ain, uint4 *rout, uint4 *aout, float &d2max, int &err,
+                                          const StencilRuns *runs, const unsigned char *col_of, int self_base)
 {
   for (int q = L.p_begin + threadIdx.x; q < L.p_end; q += blockDim.x)
   {
@@ -1080,7 +1186,8 @@ __device__ __forceinline__ void step_tile(const FastParams &Q, const FastBuffers
     const int i = q - L.p_begin;
     const short *lp = KIND == KIND_VERLET ? (list_staged ? slist + i : glist + i) : nullptr;
     if (staged)
-      gather_sums_staged<KIND, STEPPER == 2>(Q, B, srec, saux, L, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
+      gather_sums_staged<KIND, STEPPER == 2>(Q, B, srec, saux, L, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a,
+                                             runs, col_of, self_base);
     else
       gather_sums<KIND, STEPPER == 2>(Q, B, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
     d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, ri, ai, v, a, z, rout, aout, err));
@@ -1140,7 +1247,9 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_kernel(FastParams P
   __shared__ __align__(16) short slist[KIND == KIND_VERLET ? kListCap : 8];
   __shared__ __align__(8) unsigned long long mbar;
   __shared__ TileLayout L;
-  __shared__ int list_staged, list_stride;
+  __shared__ int list_staged, list_stride, self_base;
+  __shared__ StencilRuns runs[KIND == KIND_CELLS ? kRunCells : 1];
+  __shared__ unsigned char col_of[KIND == KIND_CELLS ? kTileCap : 4];
   FastControl *ctrl = B.ctrl;
   const int par = ctrl->parity;
   const uint4 *rin = par ? B.rec1 : B.rec0;
@@ -1157,6 +1266,11 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_kernel(FastParams P
   __syncthreads();
   const bool staged = L.staged;
   if (L.p_end <= L.p_begin) return;
+  const int sys = MULTI ? B.tile_sys[t] : 0;
+  const FastParams Q = MULTI ? with_system(P, B.sys[sys]) : P;
+  // cell lists: the stencil run table, built while the bulk copies land
+  const bool use_runs = KIND == KIND_CELLS && staged && L.ncols <= kRunCells;
+  if (use_runs) build_runs(L, B.cell_off + Q.cell0, Q.nc, runs, col_of, &self_base, &ctrl->error);
   const short *glist = KIND == KIND_VERLET ? B.vl + tile_list_base(P.cap, t, L.p_begin) : nullptr;
   if (staged)
   {
@@ -1170,8 +1284,6 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_kernel(FastParams P
       return;
     }
   }
-  const int sys = MULTI ? B.tile_sys[t] : 0;
-  const FastParams Q = MULTI ? with_system(P, B.sys[sys]) : P;
   float d2max = 0.0f;
   int err = 0;
   for (int q = L.p_begin + threadIdx.x; q < L.p_end; q += blockDim.x)
@@ -1188,7 +1300,8 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_kernel(FastParams P
     const int i = q - L.p_begin;
     const short *lp = KIND == KIND_VERLET ? (list_staged ? slist + i : glist + i) : nullptr;
     if (staged)
-      gather_sums_staged<KIND, STEPPER == 2>(Q, B, srec, saux, L, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
+      gather_sums_staged<KIND, STEPPER == 2>(Q, B, srec, saux, L, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a,
+                                             use_runs ? runs : nullptr, col_of, self_base);
     else
       gather_sums<KIND, STEPPER == 2>(Q, B, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
     d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, ri, ai, v, a, z, rout, aout, err));
@@ -1207,8 +1320,10 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_persistent_kernel(F
   __shared__ __align__(16) short slist[KIND == KIND_VERLET ? kListCap : 8];
   __shared__ __align__(8) unsigned long long mbar;
   __shared__ TileLayout L;
-  __shared__ int list_staged, list_stride, tile_id;
+  __shared__ int list_staged, list_stride, tile_id, self_base;
   __shared__ uint32_t phase;  // mbarrier phase of the next staged tile
+  __shared__ StencilRuns runs[KIND == KIND_CELLS ? kRunCells : 1];
+  __shared__ unsigned char col_of[KIND == KIND_CELLS ? kTileCap : 4];
   FastControl *ctrl = B.ctrl;
   const int par = ctrl->parity;
   const uint4 *rin = par ? B.rec1 : B.rec0;
@@ -1235,6 +1350,19 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_persistent_kernel(F
     const int t = tile_id;
     if (t >= P.ntiles) break;
     const bool staged = L.staged;
+    const int sys = MULTI ? B.tile_sys[t] : 0;
+    const bool use_runs = KIND == KIND_CELLS && staged && L.ncols <= kRunCells && L.p_end > L.p_begin;
+    if (use_runs)
+    {
+      if (MULTI)
+      {
+        const SysParams *S = B.sys + sys;
+        build_runs(L, B.cell_off + S->cell0, S->nc, runs, col_of, &self_base, &ctrl->error);
+      } else
+      {
+        build_runs(L, B.cell_off + P.cell0, P.nc, runs, col_of, &self_base, &ctrl->error);
+      }
+    }
     if (staged)
     {
       const uint32_t ph = phase;
@@ -1248,16 +1376,16 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_persistent_kernel(F
       if (threadIdx.x == 0) phase = ph ^ 1u;  // read again only after the next barrier
     }
     if (L.p_end <= L.p_begin) continue;
-    const int sys = MULTI ? B.tile_sys[t] : 0;
     const short *glist = KIND == KIND_VERLET ? B.vl + tile_list_base(P.cap, t, L.p_begin) : nullptr;
     float d2max = 0.0f;
     int err = 0;
     if (!MULTI)
       step_tile<MODEL, STEPPER, KIND>(P, B, L, srec, saux, slist, glist, list_staged, list_stride, staged, rin, ain,
-                                      rout, aout, d2max, err);
+                                      rout, aout, d2max, err, use_runs ? runs : nullptr, col_of, self_base);
     else
       step_tile<MODEL, STEPPER, KIND>(with_system(P, B.sys[sys]), B, L, srec, saux, slist, glist, list_staged,
-                                      list_stride, staged, rin, ain, rout, aout, d2max, err);
+                                      list_stride, staged, rin, ain, rout, aout, d2max, err,
+                                      use_runs ? runs : nullptr, col_of, self_base);
     publish_max(ctrl, B.sysctl, sys, d2max, err);
   }
 }
@@ -1345,69 +1473,76 @@ __device__ __forceinline__ double warp_sum(double v)
   return v;
 }
 
-// partial[sys * chunks + chunk] over the chunk's slots of system blockIdx.y;
-// `gated`: only after a sampling step (inside step graphs).
-__global__ void fast_order_partials_kernel(FastParams P, FastBuffers B, OrderSums *__restrict__ partial, int chunks,
-                                           int gated)
+// partial[k] = sums over chunk k (at most kOrderChunk slots of one system);
+// a small grid walks all chunks, so the gated launch that finds no sampling
+// step costs a few hundred CTAs.
+__global__ void fast_order_partials_kernel(FastParams P, FastBuffers B, OrderSums *__restrict__ partial,
+                                           const int2 *__restrict__ items, int nitems, int gated)
 {
   if (gated && !sample_now(B.ctrl)) return;
   __shared__ double sh[4][8];
-  const SysParams *S = B.sys + blockIdx.y;
-  const long begin = (long) S->first + (long) blockIdx.x * kOrderChunk;
-  const long end = min((long) S->first + S->n, begin + kOrderChunk);
   const uint4 *rec = B.ctrl->parity ? B.rec1 : B.rec0;
-  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-  for (long q = begin + threadIdx.x; q < end; q += blockDim.x)
+  for (int k = blockIdx.x; k < nitems; k += gridDim.x)
   {
-    const uint4 r = rec[q];
-    a0 += (double) __uint_as_float(r.z);
-    a1 += (double) __uint_as_float(r.w);
-    if (P.model == 2)
+    const int2 it = items[k];
+    const SysParams *S = B.sys + it.x;
+    const long begin = it.y;
+    const long end = min((long) S->first + S->n, begin + kOrderChunk);
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    for (long q = begin + threadIdx.x; q < end; q += blockDim.x)
     {
-      const float2 v = B.vel[q];
-      const double vx = v.x, vy = v.y;
-      const double m = sqrt(vx * vx + vy * vy);
-      if (m > 0.0)
+      const uint4 r = rec[q];
+      a0 += (double) __uint_as_float(r.z);
+      a1 += (double) __uint_as_float(r.w);
+      if (P.model == 2)
       {
-        a2 += vx / m;
-        a3 += vy / m;
+        const float2 v = B.vel[q];
+        const double vx = v.x, vy = v.y;
+        const double m = sqrt(vx * vx + vy * vy);
+        if (m > 0.0)
+        {
+          a2 += vx / m;
+          a3 += vy / m;
+        }
       }
     }
-  }
-  a0 = warp_sum(a0);
-  a1 = warp_sum(a1);
-  a2 = warp_sum(a2);
-  a3 = warp_sum(a3);
-  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  if ((threadIdx.x & 31) == 0)
-  {
-    sh[0][w] = a0;
-    sh[1][w] = a1;
-    sh[2][w] = a2;
-    sh[3][w] = a3;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0)
-  {
-    double t[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int k = 0; k < nw; ++k)
-      for (int c = 0; c < 4; ++c) t[c] += sh[c][k];
-    partial[(long) blockIdx.y * chunks + blockIdx.x] = OrderSums{t[0], t[1], t[2], t[3]};
+    a0 = warp_sum(a0);
+    a1 = warp_sum(a1);
+    a2 = warp_sum(a2);
+    a3 = warp_sum(a3);
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if ((threadIdx.x & 31) == 0)
+    {
+      sh[0][w] = a0;
+      sh[1][w] = a1;
+      sh[2][w] = a2;
+      sh[3][w] = a3;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+      double t[4] = {0.0, 0.0, 0.0, 0.0};
+      for (int u = 0; u < nw; ++u)
+        for (int c = 0; c < 4; ++c) t[c] += sh[c][u];
+      partial[k] = OrderSums{t[0], t[1], t[2], t[3]};
+    }
+    __syncthreads();
   }
 }
 
 // Per system: the order parameters (R, arg, R_v, arg_v) into out4 and, after a
 // sampling step, the running sums of R, R^2, R_v, R_v^2 and the sample count.
-__global__ void fast_order_finish_kernel(FastParams P, FastBuffers B, const OrderSums *__restrict__ partial, int chunks,
-                                         double *__restrict__ out4, double *__restrict__ stats, int gated)
+__global__ void fast_order_finish_kernel(FastParams P, FastBuffers B, const OrderSums *__restrict__ partial,
+                                         const int *__restrict__ first_item, double *__restrict__ out4,
+                                         double *__restrict__ stats, int gated)
 {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= P.nsys) return;
   if (gated && !sample_now(B.ctrl)) return;
   double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
-  for (int c = 0; c < chunks; ++c)
+  for (int c = first_item[r]; c < first_item[r + 1]; ++c)
   {
-    const OrderSums v = partial[(long) r * chunks + c];
+    const OrderSums v = partial[c];
     t0 += v.c;
     t1 += v.s;
     t2 += v.vx;
@@ -1685,10 +1820,24 @@ int fast_create(spss_ctx *ctx)
   SPSS_TRY(f->sysctl.reserve((size_t) f->nsys));
   SPSS_TRY(f->sys_of.reserve((size_t) n));
   {
-    int max_n = 1;
-    for (const SysParams &S : f->h_sys) max_n = std::max(max_n, S.n);
-    f->order_chunks = (max_n + kOrderChunk - 1) / kOrderChunk;
-    SPSS_TRY(f->order_partial.reserve((size_t) f->nsys * f->order_chunks));
+    std::vector<int2> items;
+    std::vector<int> first_item;
+    for (const SysParams &S : f->h_sys)
+    {
+      first_item.push_back((int) items.size());
+      for (long b = 0; b < S.n; b += kOrderChunk) items.push_back(make_int2(S.index, (int) (S.first + b)));
+    }
+    first_item.push_back((int) items.size());
+    f->order_chunks = (int) items.size();
+    f->order_grid = std::min(f->order_chunks, 4 * 152);
+    SPSS_TRY(f->order_partial.reserve((size_t) f->order_chunks));
+    SPSS_TRY(f->order_items.reserve(items.size()));
+    SPSS_TRY(f->order_first.reserve(first_item.size()));
+    SPSS_CUDA_TRY(cudaMemcpyAsync(f->order_items.ptr, items.data(), sizeof(int2) * items.size(),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    SPSS_CUDA_TRY(cudaMemcpyAsync(f->order_first.ptr, first_item.data(), sizeof(int) * first_item.size(),
+                                  cudaMemcpyHostToDevice, ctx->stream));
+    SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
     SPSS_TRY(f->order_out.reserve((size_t) f->nsys * 4));
     SPSS_TRY(f->stats.reserve((size_t) f->nsys * 5));
     SPSS_CUDA_TRY(cudaMemsetAsync(f->stats.ptr, 0, sizeof(double) * 5 * f->nsys, ctx->stream));
@@ -1763,6 +1912,8 @@ void fast_destroy(spss_ctx *ctx)
   f->tile_sys.release();
   f->sysctl.release();
   f->order_partial.release();
+  f->order_items.release();
+  f->order_first.release();
   f->order_out.release();
   f->stats.release();
   f->snap.release();
@@ -1875,12 +2026,12 @@ static int launch_sampling(spss_ctx *ctx, const FastParams &P, int gated)
 {
   FastPath *f = ctx->fast;
   const FastBuffers B = buffers(ctx);
-  fast_order_partials_kernel<<<dim3(f->order_chunks, f->nsys), 256, 0, ctx->stream>>>(P, B, f->order_partial.ptr,
-                                                                                        f->order_chunks, gated);
+  fast_order_partials_kernel<<<f->order_grid, 256, 0, ctx->stream>>>(P, B, f->order_partial.ptr,
+                                                                       f->order_items.ptr, f->order_chunks, gated);
   ++ctx->launches;
   SPSS_TRY(check_launch("fast_order_partials_kernel"));
   fast_order_finish_kernel<<<blocks_for(f->nsys, 128), 128, 0, ctx->stream>>>(
-      P, B, f->order_partial.ptr, f->order_chunks, f->order_out.ptr, f->stats.ptr, gated);
+      P, B, f->order_partial.ptr, f->order_first.ptr, f->order_out.ptr, f->stats.ptr, gated);
   ++ctx->launches;
   return check_launch("fast_order_finish_kernel");
 }
@@ -2227,7 +2378,7 @@ int fast_autotune(spss_ctx *ctx, int stepper, double dt, int steps, double *best
   const int timing = ctx->timing;
   ctx->timing = 0;
   SPSS_TRY(take_snapshot(ctx));
-  const int widths[] = {8, 16, 32, 64};
+  const int widths[] = {16, 24, 32, 40, 48, 56, 64};
   double best = 1e300;
   int best_w = f->tile_cells, best_p = f->persistent;
   int rc = SPSS_OK;
