@@ -55,7 +55,7 @@ _lib = None
 # name -> (restype, argtypes); every exported symbol of the C ABI
 P = ctypes.POINTER
 _d, _i, _l, _vp = ctypes.c_double, ctypes.c_int, ctypes.c_long, ctypes.c_void_p
-_dp, _ip = P(ctypes.c_double), P(ctypes.c_int)
+_dp, _ip, _fp = P(ctypes.c_double), P(ctypes.c_int), P(ctypes.c_float)
 _ull = ctypes.c_ulonglong
 SIGNATURES = {
     "spss_version": (_i, []),
@@ -100,7 +100,19 @@ SIGNATURES = {
     "spss_set_tiling": (_i, [_vp, _i, _i]),
     "spss_get_tiling": (_i, [_vp, _ip, _ip]),
     "spss_autotune": (_i, [_vp, _i, _d, _i, _dp]),
+    # learned surrogate (include/spss_surrogate.h)
+    "spss_mlp_create": (_i, [_ull, P(_vp)]),
+    "spss_mlp_destroy": (_i, [_vp]),
+    "spss_mlp_set_params": (_i, [_vp, _fp, _l]),
+    "spss_mlp_get_params": (_i, [_vp, _fp, _l]),
+    "spss_mlp_forward": (_i, [_vp, _fp, _l, _fp]),
+    "spss_mlp_gradient": (_i, [_vp, _fp, _fp, _fp, _l, _fp, _dp]),
+    "spss_mlp_set_data": (_i, [_vp, _fp, _fp, _l]),
+    "spss_mlp_train": (_i, [_vp, _i, _i, ctypes.c_float, _fp, _ull, _fp]),
+    "spss_mlp_kernel_launches": (_i, [_vp, P(_ull)]),
 }
+
+MLP_INPUTS, MLP_HIDDEN, MLP_OUTPUTS, MLP_PARAMS = 5, 128, 4, 34308
 
 STATS_PER_SYSTEM = 5
 
@@ -133,6 +145,10 @@ def dptr(a):
 
 def iptr(a):
     return a.ctypes.data_as(_ip)
+
+
+def fptr(a):
+    return a.ctypes.data_as(_fp)
 
 
 def f64(a):
