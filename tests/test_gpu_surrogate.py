@@ -106,3 +106,31 @@ def test_training_reduces_loss_and_is_deterministic():
     assert losses[-1] <= 0.1 * losses[0], (losses[0], losses[-1])
     assert np.array_equal(runs[0][1], runs[1][1])
     assert np.array_equal(runs[0][0], runs[1][0])
+
+
+def test_surrogate_gains_over_the_plain_simulation():
+    """What the trained network gains (small phase diagram, N = 256, 2000
+    steps): against a 64-replica reference of the expected order parameters,
+    its values are much closer than a single plain run's (median error less
+    than half), it is within 0.03 more often, and the whole diagram took fewer
+    simulated runs than the plain method needs per point for a 0.02 standard
+    error.  The judge's runs agree with the predicted mean and spread
+    (|z| <= 3 for 90 % of them)."""
+    from spsslangevinintegration_gb300 import surrogate as S
+
+    grid = S.grid_points(24, 24, n=256)
+    res = S.phase_diagram(grid, n_train=6000, steps=2000, epochs=100, rounds=1, flag_fraction=0.1, n=256)
+    rng = np.random.default_rng(0)
+    idx = rng.choice(len(grid), 16, replace=False)
+    reps = 64
+    mean, std = S.reference([grid[i] for i in idx], reps, steps=2000)
+    err_net = np.abs(res["values"][idx] - mean).max(axis=1)
+    # one plain run per point: a fresh replica of the same points
+    one = S.run_values(S.simulate([grid[i] for i in idx], steps=2000, first_replica=5 * 10 ** 6))
+    err_one = np.abs(one - mean).max(axis=1)
+    assert np.median(err_net) < 0.5 * np.median(err_one), (np.median(err_net), np.median(err_one))
+    assert np.mean(err_net <= 0.03) > np.mean(err_one <= 0.03)
+    runs_needed = np.maximum(1.0, (std.max(axis=1) / 0.02) ** 2).mean() * len(grid)
+    assert res["runs"] < runs_needed, (res["runs"], runs_needed)
+    z = np.abs(res["judge_z"])
+    assert np.mean(z.max(axis=1) <= 3.0) >= 0.9
