@@ -15,8 +15,13 @@ HBM (CUDA events on the library's stream, max over ranks, summed over ranks).
 `e2e`: the same through spss_step_host (host array in, host array out every
 step).  `roofline`: the pair-and-update kernel's algorithmic bytes over its
 CUDA-event duration.  `cpu_baseline` (rank 0): the oracle port of the
-reference algorithm on this host's cores.  `--impl reference` times the
-oracle port alone on the same workload.
+reference algorithm on this host's cores.  `sweep`: 512 independent systems
+of the batched parameter sweep stepped as one batch (phase-diagram points
+per hour at 20,000 steps per point).  `surrogate` (rank 0): a 256 x 256
+phase diagram from the learned surrogate with an active-learning round,
+checked against a replica reference, against the plain method's cost at the
+same precision.  `--impl reference` times the oracle port alone on the
+N = 4,194,304 workload.
 """
 import argparse
 import json
@@ -261,6 +266,45 @@ def run_sweep_leg(args, rank, world, barrier, max_over_ranks):
     return out
 
 
+def run_surrogate_leg(args):
+    """Phase diagram over a 256 x 256 (sigma, D) grid (N = 1024, density 2,
+    m = 1, v0 = 0.5, 4000 SE steps per run) from the learned surrogate with one
+    active-learning round, checked against a 256-replica reference at 48
+    random grid points; the plain method's cost at the same precision is the
+    measured single-run rate divided by the runs a point needs for a 0.02
+    standard error (from the reference's run-to-run spread)."""
+    from spsslangevinintegration_gb300 import surrogate as S
+
+    grid = S.grid_points(256, 256)
+    t0 = time.perf_counter()
+    res = S.phase_diagram(grid, n_train=args.surrogate_train, steps=4000, epochs=100, rounds=1, flag_fraction=0.05)
+    total = time.perf_counter() - t0
+    idx = np.random.default_rng(11).choice(len(grid), 48, replace=False)
+    mean, std = S.reference([grid[i] for i in idx], 256, steps=4000)
+    err = np.abs(res["values"][idx] - mean).max(axis=1)
+    runs_needed = float(np.maximum(1.0, (std.max(axis=1) / 0.02) ** 2).mean())
+    single_rate = args.surrogate_train / res["seconds"]["simulate_training"]  # plain runs per second
+    plain_pph = single_rate * 3600.0 / runs_needed
+    sur_pph = len(grid) * 3600.0 / total
+    z = np.abs(res["judge_z"]).max(axis=1)
+    return {
+        "workload": "256 x 256 (sigma in [0, 3], D log in [0.01, 1]) phase diagram of the expected phase and "
+                    "velocity order parameters, N=1024, density 2, m=1, v0=0.5, StochasticEuler dt=0.005, 4000 "
+                    "steps per run (time average over the second half, every 10 steps)",
+        "network": "5-128-128-128-4 GELU, BF16 operands, FP32 accumulate (tcgen05, tensor memory), Adam",
+        "training_runs": args.surrogate_train, "judge_runs": int(res["runs"] - args.surrogate_train),
+        "seconds": {k: round(v, 3) for k, v in res["seconds"].items()}, "seconds_total": total,
+        "points_per_hour": sur_pph,
+        "plain_points_per_hour_at_0.02": plain_pph,
+        "plain_runs_per_point_at_0.02": runs_needed,
+        "ratio_vs_plain": sur_pph / plain_pph,
+        "accuracy": {"reference": "48 grid points x 256 plain runs", "median_abs_error": float(np.median(err)),
+                     "q90_abs_error": float(np.quantile(err, 0.9)), "frac_within_0.02": float(np.mean(err <= 0.02))},
+        "judge_calibration": {"frac_abs_z_le_2": float(np.mean(z <= 2.0)), "frac_abs_z_le_3": float(np.mean(z <= 3.0))},
+        "network_kernel_launches": int(res["network_kernel_launches"]),
+    }
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -410,6 +454,8 @@ def run_ours(args, rank, world, local_rank):
         sw = run_sweep_leg(args, rank, world, barrier, max_over_ranks)
         if sw is not None:
             line["sweep"] = sw
+    if not args.no_surrogate and rank == 0:
+        line["surrogate"] = run_surrogate_leg(args)
     print(json.dumps(line), flush=True)
     return 0
 
@@ -425,6 +471,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--sweep-steps", type=int, default=400)
+    ap.add_argument("--no-surrogate", action="store_true")
+    ap.add_argument("--surrogate-train", type=int, default=50000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
