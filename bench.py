@@ -350,6 +350,34 @@ def run_reference(args, rank, world):
     return 0
 
 
+def run_legs_only(args, rank, world, local_rank):
+    """Only the sweep and/or surrogate legs (for profiling them alone); the
+    default run measures every leg."""
+    import torch
+
+    from spsslangevinintegration_gb300.replicas import max_over_ranks
+
+    torch.cuda.set_device(local_rank)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    line = {"legs": sorted(args.legs)}
+    if "sweep" in args.legs:
+        sw = run_sweep_leg(args, rank, world, barrier, max_over_ranks)
+        if sw is not None:
+            line["sweep"] = sw
+    if "surrogate" in args.legs and rank == 0:
+        line["surrogate"] = run_surrogate_leg(args)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
 
@@ -473,6 +501,8 @@ def main():
     ap.add_argument("--sweep-steps", type=int, default=400)
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--surrogate-train", type=int, default=50000)
+    ap.add_argument("--legs", default="main,sweep,surrogate",
+                    help="comma-separated subset of main, sweep, surrogate (profiling a leg alone)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -485,7 +515,13 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    rc = run_ours(args, rank, world, local_rank)
+    args.legs = set(x.strip() for x in args.legs.split(",") if x.strip())
+    if "main" in args.legs:
+        args.no_sweep = args.no_sweep or "sweep" not in args.legs
+        args.no_surrogate = args.no_surrogate or "surrogate" not in args.legs
+        rc = run_ours(args, rank, world, local_rank)
+    else:
+        rc = run_legs_only(args, rank, world, local_rank)
     if world > 1:
         import torch.distributed as dist
 
