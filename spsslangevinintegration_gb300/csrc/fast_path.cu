@@ -1240,7 +1240,7 @@ __device__ __forceinline__ void init_mbarrier(uint32_t mb)
 // MULTI: several systems, whose parameters come from the system table (one
 // system: from the kernel's parameter space, which costs no registers).
 template<int MODEL, int STEPPER, int KIND, bool MULTI>
-__global__ void __launch_bounds__(kTileThreads, 8) fast_tile_kernel(FastParams P, FastBuffers B)
+__global__ void __launch_bounds__(kTileThreads, 9) fast_tile_kernel(FastParams P, FastBuffers B)
 {
   __shared__ __align__(16) uint4 srec[kTileCap];
   __shared__ __align__(16) uint4 saux[kTileCap];
@@ -1299,7 +1299,12 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_kernel(FastParams P
     const uint64_t Xi = join64(ri.x, ai.x), Yi = join64(ri.y, ai.y);
     const int i = q - L.p_begin;
     const short *lp = KIND == KIND_VERLET ? (list_staged ? slist + i : glist + i) : nullptr;
-    if (staged)
+    // a staged list is walked through its shared-memory pointer, so its
+    // entries are read with shared-memory loads
+    if (staged && KIND == KIND_VERLET && list_staged)
+      gather_sums_staged<KIND, STEPPER == 2>(Q, B, srec, saux, L, rin, ain, q, cnt, slist + i, list_stride, ri, Xi,
+                                             Yi, a, nullptr, col_of, self_base);
+    else if (staged)
       gather_sums_staged<KIND, STEPPER == 2>(Q, B, srec, saux, L, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a,
                                              use_runs ? runs : nullptr, col_of, self_base);
     else
