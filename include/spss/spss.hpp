@@ -20,12 +20,14 @@
 #ifndef SPSS_DROPIN_HPP
 #define SPSS_DROPIN_HPP
 
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdio>
 #include <numeric>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../spss_gpu.h"
@@ -618,5 +620,108 @@ class BinaryObserver
   FILE *traj_ = nullptr;
   FILE *summ_ = nullptr;
 };
+
+namespace spss
+{
+
+// Binary observer on the GPU state of a system: frames in the reference's
+// .bin format ([float t][float s*n]) computed on the GPU (spss_frame_async)
+// into page-locked buffers and written by a background thread while the next
+// steps run; optional summary lines (t, |R|, arg R).  `wrapped` follows
+// BinaryObserverFirstOrder (positions and phases wrapped), otherwise
+// BinaryObserverSecondOrder (the state as it is).  No counterpart in the
+// reference beyond the file formats.
+class TrajectoryWriter
+{
+ public:
+  TrajectoryWriter(spss::SystemBase &system, int number_of_particles, int number_of_state_variables,
+                   const std::string &trajectory_file, const std::string &summary_file, int every, bool wrapped)
+      : ctx_(system.context()), len_((long) number_of_particles * number_of_state_variables), every_(every),
+        mode_(wrapped ? SPSS_FRAME_WRAPPED : SPSS_FRAME_RAW)
+  {
+    traj_ = std::fopen(trajectory_file.c_str(), "wb");
+    if (!traj_) throw std::runtime_error("TrajectoryWriter: cannot open " + trajectory_file);
+    if (!summary_file.empty()) summ_ = std::fopen(summary_file.c_str(), "w");
+    for (int b = 0; b < 2; ++b)
+      spss::check(spss_pinned_alloc(sizeof(float) * (size_t) len_, (void **) &buf_[b]), "spss_pinned_alloc");
+  }
+  TrajectoryWriter(const TrajectoryWriter &) = delete;
+  TrajectoryWriter &operator=(const TrajectoryWriter &) = delete;
+  ~TrajectoryWriter()
+  {
+    for (auto &w : writer_)
+      if (w.joinable()) w.join();
+    for (float *b : buf_)
+      if (b) spss_pinned_free(b);
+    if (traj_) std::fclose(traj_);
+    if (summ_) std::fclose(summ_);
+  }
+  void operator()(Real t)
+  {
+    if (!(counter_++ % every_))
+    {
+      const int b = next_;
+      if (writer_[b].joinable()) writer_[b].join();  // this buffer's previous frame is on disk
+      spss::check(spss_frame_async(ctx_, mode_, buf_[b], len_), "spss_frame_async");
+      if (summ_)
+      {
+        double r[4];
+        spss::check(spss_order_parameters(ctx_, r), "spss_order_parameters");  // synchronises the stream
+        std::fprintf(summ_, "%g\t%g\t%g\n", (float) t, (float) r[0], (float) r[1]);
+      } else
+      {
+        spss::check(spss_synchronize(ctx_), "spss_synchronize");
+      }
+      // frames reach the file in order: the previous frame's writer finishes first
+      if (writer_[1 - b].joinable()) writer_[1 - b].join();
+      const float tf = (float) t;
+      float *frame = buf_[b];
+      FILE *f = traj_;
+      const long len = len_;
+      writer_[b] = std::thread([f, tf, frame, len]() {
+        std::fwrite(&tf, sizeof(float), 1, f);
+        std::fwrite(frame, sizeof(float), (size_t) len, f);
+      });
+      next_ = 1 - b;
+    }
+  }
+
+ private:
+  spss_ctx *ctx_;
+  long len_;
+  int every_, mode_;
+  int counter_ = 0, next_ = 0;
+  float *buf_[2] = {nullptr, nullptr};
+  std::thread writer_[2];
+  FILE *traj_ = nullptr;
+  FILE *summ_ = nullptr;
+};
+
+// The last frame of a .bin trajectory file as the initial state
+// (SimulationEngineFirstOrder::InitializeSystemStateFromPreviousSolution,
+// SimulationEngineFirstOrder.cpp:69-93); returns the frame's time.
+inline Real ReadLastFrame(const std::string &file, int number_of_particles, int number_of_state_variables, Real *state)
+{
+  FILE *f = std::fopen(file.c_str(), "rb");
+  if (!f) throw std::runtime_error("ReadLastFrame: cannot open " + file);
+  const long per = 1L + (long) number_of_particles * number_of_state_variables;
+  std::fseek(f, 0, SEEK_END);
+  const long size = std::ftell(f);
+  const long frames = size / (per * (long) sizeof(float));
+  if (frames < 1)
+  {
+    std::fclose(f);
+    throw std::runtime_error("ReadLastFrame: no whole frame in " + file);
+  }
+  std::fseek(f, (frames - 1) * per * (long) sizeof(float), SEEK_SET);
+  std::vector<float> raw((size_t) per);
+  const size_t got = std::fread(raw.data(), sizeof(float), (size_t) per, f);
+  std::fclose(f);
+  if (got != (size_t) per) throw std::runtime_error("ReadLastFrame: short read from " + file);
+  std::copy(raw.begin() + 1, raw.end(), state);
+  return (Real) raw[0];
+}
+
+}  // namespace spss
 
 #endif

@@ -128,6 +128,23 @@ int spss_apply_pbc(spss_ctx *ctx);
  * BinaryObserverSecondOrder.cpp:121-138), accumulated in FP64:
  * out = {|<e^{i phi}>|, arg, |<v/|v|>|, arg}; first order repeats the phase pair. */
 int spss_order_parameters(spss_ctx *ctx, double *out4);
+/* One trajectory frame of the reference's binary observers, the s*n floats
+ * that follow the float time stamp in their .bin files: SPSS_FRAME_WRAPPED as
+ * BinaryObserverFirstOrder::SaveSystemState (BinaryObserverFirstOrder.cpp:101-123:
+ * the state converted to float, positions wrapped into the unit box and the
+ * phase into [0, 2 pi), with the reference's float/double rounding steps),
+ * SPSS_FRAME_RAW as BinaryObserverSecondOrder::SaveSystemState
+ * (BinaryObserverSecondOrder.cpp:101-116: the state converted to float).  The
+ * frame is computed on the GPU and copied to `dst` (len = s*n floats) on the
+ * context's stream; the call returns without synchronising, so `dst` must stay
+ * valid until spss_synchronize (pinned memory from spss_pinned_alloc makes the
+ * copy asynchronous; pageable memory works too, with a staged copy). */
+#define SPSS_FRAME_RAW 0
+#define SPSS_FRAME_WRAPPED 1
+int spss_frame_async(spss_ctx *ctx, int mode, float *dst, long len);
+/* Page-locked host memory for frames (cudaMallocHost / cudaFreeHost). */
+int spss_pinned_alloc(size_t bytes, void **out);
+int spss_pinned_free(void *p);
 /* AveragingObserver::operator() and the averaged state (AveragingObserver.cpp:29-69). */
 int spss_average_accumulate(spss_ctx *ctx);
 int spss_average_get(spss_ctx *ctx, double *mean_state, long len, int *count);

@@ -16,6 +16,7 @@ ERR_INVALID_ARGUMENT, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_NOT_SUPPORTED, ERR_NONFIN
 
 VARIANT_DISPATCH, ALL_PAIRS, LINKED_LIST, VERLET, LINKED_LIST_VERLET, GLOBAL_FIELD = range(6)
 PRECISION_F64, PRECISION_F32 = 0, 1
+FRAME_RAW, FRAME_WRAPPED = 0, 1
 RK4, STOCHASTIC_EULER, STOCHASTIC_RUNGE_KUTTA = 0, 1, 2
 
 
@@ -100,6 +101,9 @@ SIGNATURES = {
     "spss_set_tiling": (_i, [_vp, _i, _i]),
     "spss_get_tiling": (_i, [_vp, _ip, _ip]),
     "spss_autotune": (_i, [_vp, _i, _d, _i, _dp]),
+    "spss_frame_async": (_i, [_vp, _i, _fp, _l]),
+    "spss_pinned_alloc": (_i, [ctypes.c_size_t, P(_vp)]),
+    "spss_pinned_free": (_i, [_vp]),
     # learned surrogate (include/spss_surrogate.h)
     "spss_mlp_create": (_i, [_ull, P(_vp)]),
     "spss_mlp_destroy": (_i, [_vp]),

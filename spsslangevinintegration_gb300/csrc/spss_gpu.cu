@@ -131,6 +131,34 @@ int order_parameters_aos(spss_ctx *ctx, const double *d_aos, double out[4])
   return SPSS_OK;
 }
 
+// One observer frame from an AoS FP64 state, element by element as the
+// reference's observers compute it: the float conversion, then (wrapped) the
+// unit-box wrap `x -= floor(x * 1) * 1` and the phase wrap
+// `phi -= floor(phi / 2 pi) * 2 pi`, both evaluated in double on the float
+// value and rounded back to float (BinaryObserverFirstOrder.cpp:112-117,
+// PeriodicBoundaryConditions.cpp:137-145).  Every rounding is explicit.
+__global__ void frame_kernel(const double *__restrict__ x, long n, int s, int model, int wrap, float *__restrict__ out)
+{
+  const long i = (long) blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int ip = model == 1 ? 2 : 4;
+  const double two_pi = 6.283185307179586;
+  for (int k = 0; k < s; ++k)
+  {
+    float v = __double2float_rn(x[(long) s * i + k]);
+    if (wrap && k < 2)
+    {
+      const double d = (double) v;
+      v = __double2float_rn(__dsub_rn(d, floor(d)));
+    } else if (wrap && k == ip)
+    {
+      const double d = (double) v;
+      v = __double2float_rn(__dsub_rn(d, __dmul_rn(floor(__ddiv_rn(d, two_pi)), two_pi)));
+    }
+    out[(long) s * i + k] = v;
+  }
+}
+
 __global__ void accumulate_kernel(double *__restrict__ acc, const double *__restrict__ x, long len)
 {
   const long q = (long) blockIdx.x * blockDim.x + threadIdx.x;
@@ -252,6 +280,8 @@ int spss_destroy(spss_ctx *ctx)
   ctx->scratch_a.release();
   ctx->scratch_b.release();
   ctx->scratch_c.release();
+  ctx->frame_state.release();
+  ctx->frame.release();
   ctx->average.release();
   if (ctx->registered_host) cudaHostUnregister(ctx->registered_host);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
@@ -642,6 +672,52 @@ int spss_get_timing(spss_ctx *ctx, double *kernel_ms, unsigned long long *timed_
   if (!ctx) return SPSS_ERR_INVALID_ARGUMENT;
   if (kernel_ms) *kernel_ms = ctx->timing_ms;
   if (timed_launches) *timed_launches = ctx->timing_count;
+  return SPSS_OK;
+}
+
+// ------------------------------------------------ trajectory frames
+
+int spss_frame_async(spss_ctx *ctx, int mode, float *dst, long len)
+{
+  if (!ctx || !dst || (mode != SPSS_FRAME_RAW && mode != SPSS_FRAME_WRAPPED)) return SPSS_ERR_INVALID_ARGUMENT;
+  if (len != state_len(ctx)) return SPSS_ERR_SIZE;
+  const double *aos = nullptr;
+  if (is_f64(ctx))
+  {
+    SPSS_TRY(f64_state_ptr(ctx, &aos));
+  } else
+  {
+    SPSS_TRY(ctx->frame_state.reserve(len));
+    SPSS_TRY(fast_get_state(ctx, ctx->frame_state.ptr));
+    aos = ctx->frame_state.ptr;
+  }
+  SPSS_TRY(ctx->frame.reserve(len));
+  const long n = ctx->p.n;
+  frame_kernel<<<(int) ((n + 255) / 256), 256, 0, ctx->stream>>>(aos, n, ctx->s, ctx->p.model,
+                                                                   mode == SPSS_FRAME_WRAPPED ? 1 : 0, ctx->frame.ptr);
+  ++ctx->launches;
+  SPSS_TRY(check_launch("frame_kernel"));
+  SPSS_CUDA_TRY(cudaMemcpyAsync(dst, ctx->frame.ptr, sizeof(float) * len, cudaMemcpyDefault, ctx->stream));
+  return SPSS_OK;
+}
+
+int spss_pinned_alloc(size_t bytes, void **out)
+{
+  if (!out || bytes == 0) return SPSS_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  if (cudaMallocHost(out, bytes) != cudaSuccess)
+  {
+    cudaGetLastError();
+    *out = nullptr;
+    return SPSS_ERR_OUT_OF_MEMORY;
+  }
+  return SPSS_OK;
+}
+
+int spss_pinned_free(void *p)
+{
+  if (!p) return SPSS_ERR_INVALID_ARGUMENT;
+  SPSS_CUDA_TRY(cudaFreeHost(p));
   return SPSS_OK;
 }
 

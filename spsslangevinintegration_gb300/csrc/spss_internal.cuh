@@ -246,6 +246,9 @@ struct spss_ctx
   int average_count = 0;
   // AoS staging buffers for host-array entry points
   spss::DeviceArray<double> scratch_a, scratch_b, scratch_c;
+  // trajectory frames (spss_frame_async): the AoS state of a fast context and the float frame
+  spss::DeviceArray<double> frame_state;
+  spss::DeviceArray<float> frame;
 };
 
 namespace spss

@@ -5,7 +5,8 @@
 // checks the written states against the oracle.
 //
 // usage: dropin_example <dir>   reads <dir>/fo_init.bin, <dir>/so_init.bin
-//                                writes fo_final.bin, so_final.bin, so_noise.bin
+//                                writes fo_final.bin, so_final.bin, so_noise.bin,
+//                                fo_traj.bin, fo_summary.txt, fo_restart.bin
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -43,12 +44,22 @@ int main(int argc, char **argv)
       RungeKutta4Stepper stepper(&thread, n, s);
       std::vector<Real> x = read_all(dir + "/fo_init.bin", (size_t) n * s);
       Real t = 0.0, dt = 0.01;
-      for (int k = 0; k < 10; ++k)
       {
-        t += dt;
-        stepper.DoStep(system, x, t, dt);
+        // the binary observer every 2 steps, wrapped as the first-order observer
+        spss::TrajectoryWriter writer(system, n, s, dir + "/fo_traj.bin", dir + "/fo_summary.txt", 2, true);
+        for (int k = 0; k < 10; ++k)
+        {
+          t += dt;
+          stepper.DoStep(system, x, t, dt);
+          writer(t);
+        }
       }
       write_all(dir + "/fo_final.bin", x);
+      // restart from the last frame written
+      std::vector<Real> restart((size_t) n * s);
+      const Real t_last = spss::ReadLastFrame(dir + "/fo_traj.bin", n, s, restart.data());
+      restart.push_back(t_last);
+      write_all(dir + "/fo_restart.bin", restart);
       if (!system.uses_verlet_list_) throw std::runtime_error("uses_verlet_list_ not set");
     }
     {

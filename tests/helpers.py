@@ -90,3 +90,22 @@ def params(model, n, density=2.0, R=1.0, v0=0.5, m=1.0, D=0.1, sigma=1.0, alpha=
     else:
         p.update(xi_r=1.0 / m, xi_phi=1.0 / m, D_r=1e-3 / L ** 2, D_phi=D / m ** 2)
     return p
+
+
+def reference_frame(x, s, wrapped):
+    """The frame a reference binary observer writes for the FP64 AoS state x:
+    float conversion, then (wrapped, first-order observer) the unit-box wrap
+    and the phase wrap evaluated in double on the float value and rounded back
+    (BinaryObserverFirstOrder.cpp:111-117, PeriodicBoundaryConditions.cpp:137-145)."""
+    f = np.asarray(x, dtype=np.float64).astype(np.float32).reshape(-1, s)
+    if wrapped:
+        out = f.copy()
+        for k in (0, 1):
+            d = f[:, k].astype(np.float64)
+            out[:, k] = (d - np.floor(d * 1.0) * 1.0).astype(np.float32)
+        ip = 2 if s == 4 else 4
+        d = f[:, ip].astype(np.float64)
+        two_pi = 6.283185307179586
+        out[:, ip] = (d - np.floor(d / two_pi) * two_pi).astype(np.float32)
+        f = out
+    return f.reshape(-1)

@@ -8,7 +8,8 @@ import tempfile
 import numpy as np
 import pytest
 
-from helpers import per_component_close
+from helpers import per_component_close, reference_frame
+from spsslangevinintegration_gb300.observers import read_frames
 
 pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -20,7 +21,7 @@ def build_example(out):
     lib = build.build_library()
     exe = os.path.join(out, "dropin_example")
     subprocess.run(["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"),
-                    os.path.join(ROOT, "tests", "cpp", "dropin_example.cpp"), "-o", exe,
+                    os.path.join(ROOT, "tests", "cpp", "dropin_example.cpp"), "-o", exe, "-pthread",
                     "-L" + os.path.dirname(lib), "-lspss_gpu", "-Wl,-rpath," + os.path.dirname(lib)], check=True)
     return exe
 
@@ -40,13 +41,29 @@ def test_dropin_classes_match_oracle():
         fo_gpu = np.fromfile(os.path.join(d, "fo_final.bin"))
         so_gpu = np.fromfile(os.path.join(d, "so_final.bin"))
         noise = np.fromfile(os.path.join(d, "so_noise.bin"))
+        times, frames = read_frames(os.path.join(d, "fo_traj.bin"), 400, 4)
+        summary = np.loadtxt(os.path.join(d, "fo_summary.txt"))
+        restart = np.fromfile(os.path.join(d, "fo_restart.bin"))
 
     sysm = ob.System(1, 400, 0.1, v0=0.3, xi=0.1, sigma=1.0, alpha=0.2, D_phi=0.1, flavor=0)
     x, t = fo.copy(), 0.0
-    for _ in range(10):
+    expected = []
+    for k in range(10):
         t += 0.01
         sysm.step(ob.RK4, 0, x, t, 0.01)
+        if k % 2 == 0:
+            expected.append((t, reference_frame(x, 4, wrapped=True)))
     per_component_close(fo_gpu, x, 4, 1e-11, "first-order RK4 drop-in")
+    # the trajectory file: 5 frames in the reference's format, each the
+    # float frame of the state (1 float ulp: the states agree to 1e-11)
+    assert len(times) == 5
+    np.testing.assert_array_equal(times, np.array([e[0] for e in expected], dtype=np.float32))
+    for got, (_, ref) in zip(frames, expected):
+        np.testing.assert_allclose(got, ref, rtol=2.5e-7, atol=1e-7)
+    assert summary.shape == (5, 3)
+    # restart reads the last frame back
+    np.testing.assert_array_equal(restart[:-1], frames[-1].astype(np.float64))
+    assert restart[-1] == np.float64(times[-1])
 
     sysm = ob.System(2, 500, 0.07, v0=0.5, xi_r=1.0, D_r=0.02, xi_phi=1.0, D_phi=0.1, sigma=1.0, flavor=0)
     x, t = so.copy(), 0.0
