@@ -80,6 +80,7 @@ struct SysParams
 enum Kind
 {
   KIND_ALL_PAIRS = 0,
+  KIND_GLOBAL = 3,  // global polar order field (first order): no lists, slot = original index
   KIND_CELLS = 1,
   KIND_VERLET = 2
 };
@@ -114,6 +115,9 @@ struct FastBuffers
   const int *order;
   short *vl;
   int *vl_cnt;
+  float *nu;             // natural frequencies (global field), slot = original index
+  double *field;         // Z = <e^{i phi}>, W = <omega e^{i phi}> and derived values (global field)
+  double *field_partial; // block partials of the field sums
   const SysParams *sys;  // system table
   const int *sys_of;     // system of each slot (equivalently of each original index)
   const int *tile_sys;   // system of each tile
@@ -176,6 +180,8 @@ struct FastPath
   DeviceArray<SysParams> sys;
   DeviceArray<int> sys_of, tile_sys;
   DeviceArray<SysControl> sysctl;
+  DeviceArray<float> nu;
+  DeviceArray<double> field, field_partial;
   std::vector<SysParams> h_sys;
   int nsys = 1;
   int total_cells = 1;
@@ -993,21 +999,17 @@ __device__ __forceinline__ void draw_noise(const FastParams &P, unsigned long lo
   }
 }
 
-// Derivative from the neighbour sums, SE or SRK update in fixed point, new
-// record.  Returns |dr|^2 of the step.
-template<int MODEL, int STEPPER>
-__device__ __forceinline__ float update_particle(const FastParams &P, const FastBuffers &B, int q, const uint4 &ri,
-                                                 const uint4 &ai, float2 v, const Acc &a, const float z[6],
-                                                 uint4 *rout, uint4 *aout, int &err)
+// Torque derivative f_w and (SRK) complementary force C from the neighbour
+// sums.  Every rounding step is spelled out (fmaf, __fmul_rn, __fadd_rn): the
+// compiler cannot contract or reassociate, so each instantiation (one system
+// or a batch) rounds identically.
+template<int STEPPER>
+__device__ __forceinline__ void sums_forces(const FastParams &P, const Acc &a, float cphi, float sphi, float wi,
+                                            float &f_w, float &C)
 {
-  const uint64_t Xi = join64(ri.x, ai.x), Yi = join64(ri.y, ai.y);
-  const float cphi = __uint_as_float(ri.z), sphi = __uint_as_float(ri.w);
-  const float wi = __uint_as_float(ai.w);
-  // Every rounding step is spelled out (fmaf, __fmul_rn, __fadd_rn): the
-  // compiler cannot contract or reassociate, so each instantiation of this
-  // function (one system or a batch) rounds identically.
   // sum sin(phi_j - phi_i - alpha) and sum (omega_j - omega_i) cos(phi_j - phi_i - alpha)
-  float f_w = 0.0f, C = 0.0f;  // SE/SRK zero-fill the derivative: an isolated particle keeps 0
+  f_w = 0.0f;  // SE/SRK zero-fill the derivative: an isolated particle keeps 0
+  C = 0.0f;
   if (a.card > 0)
   {
     const float inv = 1.0f / (float) a.card;
@@ -1022,6 +1024,35 @@ __device__ __forceinline__ float update_particle(const FastParams &P, const Fast
                                                        __fmul_rn(wi, fmaf(P.ca, K, __fmul_rn(P.sa, S)))));
     }
   }
+}
+
+template<int MODEL, int STEPPER>
+__device__ __forceinline__ float advance_particle(const FastParams &P, const FastBuffers &B, int q, const uint4 &ri,
+                                                  const uint4 &ai, float2 v, float f_w, float C, const float z[6],
+                                                  uint4 *rout, uint4 *aout, int &err);
+
+// Derivative from the neighbour sums, SE or SRK update in fixed point, new
+// record.  Returns |dr|^2 of the step.
+template<int MODEL, int STEPPER>
+__device__ __forceinline__ float update_particle(const FastParams &P, const FastBuffers &B, int q, const uint4 &ri,
+                                                 const uint4 &ai, float2 v, const Acc &a, const float z[6],
+                                                 uint4 *rout, uint4 *aout, int &err)
+{
+  float f_w, C;
+  sums_forces<STEPPER>(P, a, __uint_as_float(ri.z), __uint_as_float(ri.w), __uint_as_float(ai.w), f_w, C);
+  return advance_particle<MODEL, STEPPER>(P, B, q, ri, ai, v, f_w, C, z, rout, aout, err);
+}
+
+// SE or SRK update in fixed point from the forces, new record.  Returns
+// |dr|^2 of the step.
+template<int MODEL, int STEPPER>
+__device__ __forceinline__ float advance_particle(const FastParams &P, const FastBuffers &B, int q, const uint4 &ri,
+                                                  const uint4 &ai, float2 v, float f_w, float C, const float z[6],
+                                                  uint4 *rout, uint4 *aout, int &err)
+{
+  const uint64_t Xi = join64(ri.x, ai.x), Yi = join64(ri.y, ai.y);
+  const float cphi = __uint_as_float(ri.z), sphi = __uint_as_float(ri.w);
+  const float wi = __uint_as_float(ai.w);
   const float dt = P.dt;
   float ddx, ddy, dphi, dw;
   if (MODEL == 1)
@@ -1580,11 +1611,132 @@ __global__ void fast_order_finish_kernel(FastParams P, FastBuffers B, const Orde
   }
 }
 
+// ---------------------------------------------------------------- global polar order field
+//
+// EvaluateInteractionsWithGlobalPolarOrderField (ParticleSystemFirstOrderPtr.cpp:155-223):
+// every particle couples to Z = <e^{i phi}> (and, for the complementary force
+// of the SRK stepper, to W = <omega e^{i phi}>), both summed in FP64 over the
+// stage state; no lists.
+
+constexpr int kFieldBlocks = 304;
+
+__global__ void fast_field_partials_kernel(FastParams P, FastBuffers B)
+{
+  __shared__ double sh[4][8];
+  const int par = B.ctrl->parity;
+  const uint4 *rec = par ? B.rec1 : B.rec0;
+  const uint4 *aux = par ? B.aux1 : B.aux0;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < P.n; q += gridDim.x * blockDim.x)
+  {
+    const double c = (double) __uint_as_float(rec[q].z), sn = (double) __uint_as_float(rec[q].w);
+    const double w = (double) __uint_as_float(aux[q].w);
+    a0 += c;
+    a1 += sn;
+    a2 += w * c;
+    a3 += w * sn;
+  }
+  a0 = warp_sum(a0);
+  a1 = warp_sum(a1);
+  a2 = warp_sum(a2);
+  a3 = warp_sum(a3);
+  const int wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if ((threadIdx.x & 31) == 0)
+  {
+    sh[0][wid] = a0;
+    sh[1][wid] = a1;
+    sh[2][wid] = a2;
+    sh[3][wid] = a3;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    double t[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int k = 0; k < nw; ++k)
+      for (int c = 0; c < 4; ++c) t[c] += sh[c][k];
+    for (int c = 0; c < 4; ++c) B.field_partial[4 * blockIdx.x + c] = t[c];
+  }
+}
+
+// field = {Re Z, Im Z, |Z|, Re W, Im W, |W|, cos arg W, sin arg W}
+__global__ void fast_field_finish_kernel(FastParams P, FastBuffers B)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double t[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int b = 0; b < kFieldBlocks; ++b)
+    for (int c = 0; c < 4; ++c) t[c] += B.field_partial[4 * b + c];
+  const double zr = t[0] / P.n, zi = t[1] / P.n, wr = t[2] / P.n, wi = t[3] / P.n;
+  const double aw = atan2(wi, wr);  // arg 0 = 0, as std::arg
+  B.field[0] = zr;
+  B.field[1] = zi;
+  B.field[2] = sqrt(zr * zr + zi * zi);
+  B.field[3] = wr;
+  B.field[4] = wi;
+  B.field[5] = sqrt(wr * wr + wi * wi);
+  B.field[6] = cos(aw);
+  B.field[7] = sin(aw);
+}
+
+// One SE or SRK step of the first-order model in the global field:
+// k[3] = -xi omega + nu_i + sigma |Z| (sin(arg Z - phi) cos a - cos(arg Z - phi) sin a)
+// and the complementary force as the reference computes it, whose last term
+// takes sin(arg W - phi) (ParticleSystemFirstOrderPtr.cpp:213-219).
+template<int STEPPER>
+__global__ void __launch_bounds__(kTB, 4) fast_global_step_kernel(FastParams P, FastBuffers B)
+{
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  FastControl *ctrl = B.ctrl;
+  const int par = ctrl->parity;
+  const uint4 *rin = par ? B.rec1 : B.rec0;
+  const uint4 *ain = par ? B.aux1 : B.aux0;
+  uint4 *rout = par ? B.rec0 : B.rec1;
+  uint4 *aout = par ? B.aux0 : B.aux1;
+  float d2max = 0.0f;
+  int err = 0;
+  if (q < P.n)
+  {
+    const unsigned p = B.pid[q];
+    const uint4 ri = rin[q];
+    const uint4 ai = ain[q];
+    float z[6];
+    draw_noise<1, STEPPER>(P, ctrl->step, p, z);
+    const float zr = (float) B.field[0], zi = (float) B.field[1], az = (float) B.field[2];
+    const float wr = (float) B.field[3], wim = (float) B.field[4], aw = (float) B.field[5];
+    const float cw = (float) B.field[6], sw = (float) B.field[7];
+    const float cphi = __uint_as_float(ri.z), sphi = __uint_as_float(ri.w), wi = __uint_as_float(ai.w);
+    const float SZ = fmaf(zi, cphi, -__fmul_rn(zr, sphi));  // |Z| sin(arg Z - phi)
+    const float KZ = fmaf(zr, cphi, __fmul_rn(zi, sphi));   // |Z| cos(arg Z - phi)
+    const float f_w = fmaf(-P.xi_phi, wi, __fadd_rn(B.nu[q], __fmul_rn(P.sigma, fmaf(P.ca, SZ, -__fmul_rn(P.sa, KZ)))));
+    float C = 0.0f;
+    if (STEPPER == 2)
+    {
+      const float KW = fmaf(wr, cphi, __fmul_rn(wim, sphi));   // |W| cos(arg W - phi)
+      const float sWp = fmaf(sw, cphi, -__fmul_rn(cw, sphi));  // sin(arg W - phi)
+      const float first = fmaf(P.ca, KW, __fmul_rn(P.sa, __fmul_rn(aw, sWp)));
+      const float second = __fmul_rn(wi, fmaf(P.ca, KZ, __fmul_rn(P.sa, __fmul_rn(az, sWp))));
+      C = __fmul_rn(P.sigma, __fsub_rn(first, second));
+    }
+    d2max = advance_particle<1, STEPPER>(P, B, q, ri, ai, make_float2(0.f, 0.f), f_w, C, z, rout, aout, err);
+  }
+  publish_max(ctrl, B.sysctl, 0, d2max, err);
+}
+
+__global__ void fast_set_frequencies_kernel(const double *__restrict__ freqs, int n, float *__restrict__ nu)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) nu[i] = (float) freqs[i];
+}
+
 // ---------------------------------------------------------------- host side
 
 static int blocks_for(long n, int tb)
 {
   return (int) ((n + tb - 1) / tb);
+}
+
+static bool has_cells(int kind)
+{
+  return kind == KIND_CELLS || kind == KIND_VERLET;
 }
 
 static FastBuffers buffers(spss_ctx *ctx)
@@ -1616,6 +1768,9 @@ static FastBuffers buffers(spss_ctx *ctx)
   B.sys_of = f->sys_of.ptr;
   B.tile_sys = f->tile_sys.ptr;
   B.sysctl = f->sysctl.ptr;
+  B.nu = f->nu.ptr;
+  B.field = f->field.ptr;
+  B.field_partial = f->field_partial.ptr;
   B.ctrl = f->ctrl;
   return B;
 }
@@ -1709,7 +1864,7 @@ static FastParams params(spss_ctx *ctx, double dt)
 static int set_tiling(spss_ctx *ctx, int tile_cells)
 {
   FastPath *f = ctx->fast;
-  if (f->kind == KIND_ALL_PAIRS) return SPSS_OK;
+  if (f->kind == KIND_ALL_PAIRS || f->kind == KIND_GLOBAL) return SPSS_OK;
   f->tile_cells = tile_cells;
   int ntiles = 0;
   std::vector<int> tile_sys;
@@ -1788,8 +1943,14 @@ int fast_create(spss_ctx *ctx)
         k = KIND_VERLET;
         grid = nc_verlet;
         break;
+      case SPSS_VARIANT_GLOBAL_FIELD:
+        // the reference's global field belongs to the first-order model; one system
+        if (q.model != 1 || systems.size() != 1) return SPSS_ERR_NOT_SUPPORTED;
+        k = KIND_GLOBAL;
+        grid = 1;
+        break;
       default:
-        return SPSS_ERR_NOT_SUPPORTED;  // global field: FP64 contexts
+        return SPSS_ERR_NOT_SUPPORTED;
     }
     if (kind >= 0 && k != kind) return SPSS_ERR_NOT_SUPPORTED;  // one list kind per context
     kind = k;
@@ -1802,6 +1963,13 @@ int fast_create(spss_ctx *ctx)
   if (first != n) return SPSS_ERR_INVALID_ARGUMENT;
   f->kind = kind;
   f->total_cells = cell0;
+  if (kind == KIND_GLOBAL)
+  {
+    SPSS_TRY(f->nu.reserve((size_t) n));
+    SPSS_TRY(f->field.reserve(8));
+    SPSS_TRY(f->field_partial.reserve(4 * kFieldBlocks));
+    SPSS_CUDA_TRY(cudaMemsetAsync(f->nu.ptr, 0, sizeof(float) * n, ctx->stream));
+  }
   f->nc_build = f->h_sys[0].nc;
   if (f->kind == KIND_VERLET) ctx->uses_verlet_list = 1;
   for (int b = 0; b < 2; ++b)
@@ -1916,6 +2084,9 @@ void fast_destroy(spss_ctx *ctx)
   f->sys_of.release();
   f->tile_sys.release();
   f->sysctl.release();
+  f->nu.release();
+  f->field.release();
+  f->field_partial.release();
   f->order_partial.release();
   f->order_items.release();
   f->order_first.release();
@@ -1935,7 +2106,7 @@ static int launch_rebuild(spss_ctx *ctx, const FastParams &P)
   FastPath *f = ctx->fast;
   const FastBuffers B = buffers(ctx);
   const int n = P.n;
-  if (f->kind != KIND_ALL_PAIRS)
+  if (has_cells(f->kind))
   {
     fast_cells_kernel<<<blocks_for(n, kTB), kTB, 0, ctx->stream>>>(P, B);
     ++ctx->launches;
@@ -1949,10 +2120,10 @@ static int launch_rebuild(spss_ctx *ctx, const FastParams &P)
     ++ctx->launches;
     SPSS_TRY(check_launch("fast_copyback_kernel"));
   }
-  fast_after_rebuild_kernel<<<1, 1, 0, ctx->stream>>>(f->ctrl, f->kind != KIND_ALL_PAIRS);
+  fast_after_rebuild_kernel<<<1, 1, 0, ctx->stream>>>(f->ctrl, has_cells(f->kind));
   ++ctx->launches;
   SPSS_TRY(check_launch("fast_after_rebuild_kernel"));
-  if (f->kind != KIND_ALL_PAIRS)
+  if (has_cells(f->kind))
   {
     fast_tile_layout_kernel<<<blocks_for(f->ntiles, 128), 128, 0, ctx->stream>>>(P, buffers(ctx));
     ++ctx->launches;
@@ -1989,7 +2160,16 @@ static void launch_step_kind(spss_ctx *ctx, const FastParams &P, const FastBuffe
 {
   const int grid = blocks_for(P.n, kTB);
   const int tiles = P.persistent ? std::min(P.ntiles, ctx->fast->persistent_grid) : P.ntiles;
-  if (ctx->fast->kind == KIND_ALL_PAIRS)
+  if (ctx->fast->kind == KIND_GLOBAL)
+  {
+    if (MODEL == 1)
+    {
+      fast_field_partials_kernel<<<kFieldBlocks, 256, 0, ctx->stream>>>(P, B);
+      fast_field_finish_kernel<<<1, 32, 0, ctx->stream>>>(P, B);
+      fast_global_step_kernel<STEPPER><<<grid, kTB, 0, ctx->stream>>>(P, B);
+      ctx->launches += 2;
+    }
+  } else if (ctx->fast->kind == KIND_ALL_PAIRS)
   {
     if (P.nsys > 1) fast_step_kernel<MODEL, STEPPER, KIND_ALL_PAIRS, true><<<grid, kTB, 0, ctx->stream>>>(P, B);
     else fast_step_kernel<MODEL, STEPPER, KIND_ALL_PAIRS, false><<<grid, kTB, 0, ctx->stream>>>(P, B);
@@ -2194,7 +2374,7 @@ static int run_steps(spss_ctx *ctx, int stepper, double dt, long nsteps, int sam
     return sampling ? sync_control(ctx) : SPSS_OK;
   }
   SPSS_TRY(push_host_control(ctx));
-  if (!f->binner.offsets.ptr && f->kind != KIND_ALL_PAIRS)
+  if (!f->binner.offsets.ptr && has_cells(f->kind))
   {
     SPSS_TRY(fast_step(ctx, stepper, 0.0, dt));
     if (sampling) SPSS_TRY(launch_sampling(ctx, params(ctx, dt), 1));
@@ -2375,7 +2555,7 @@ int fast_autotune(spss_ctx *ctx, int stepper, double dt, int steps, double *best
   FastPath *f = ctx->fast;
   if (!f->have_state || steps < 1) return SPSS_ERR_INVALID_ARGUMENT;
   if (stepper == SPSS_STEPPER_RK4) return SPSS_ERR_NOT_SUPPORTED;
-  if (f->kind == KIND_ALL_PAIRS)
+  if (!has_cells(f->kind))
   {
     if (best_ms) *best_ms = 0.0;
     return SPSS_OK;
@@ -2417,6 +2597,15 @@ int fast_autotune(spss_ctx *ctx, int stepper, double dt, int steps, double *best
   if (rc3 != SPSS_OK) return rc3;
   if (best_ms) *best_ms = best;
   return SPSS_OK;
+}
+
+int fast_set_natural_frequencies(spss_ctx *ctx, const double *d_freqs)
+{
+  FastPath *f = ctx->fast;
+  if (f->kind != KIND_GLOBAL) return SPSS_ERR_NOT_SUPPORTED;  // the reference uses them in the global field only
+  fast_set_frequencies_kernel<<<blocks_for(ctx->p.n, kTB), kTB, 0, ctx->stream>>>(d_freqs, ctx->p.n, f->nu.ptr);
+  ++ctx->launches;
+  return check_launch("fast_set_frequencies_kernel");
 }
 
 int fast_noise(spss_ctx *ctx, int stepper, unsigned long long step, double *d_out)

@@ -357,9 +357,9 @@ int spss_set_natural_frequencies(spss_ctx *ctx, const double *freqs, long len)
 {
   if (!ctx || !freqs) return SPSS_ERR_INVALID_ARGUMENT;
   if (len != ctx->p.n) return SPSS_ERR_SIZE;
-  if (!is_f64(ctx)) return SPSS_ERR_NOT_SUPPORTED;
   SPSS_TRY(upload(ctx, ctx->scratch_a, freqs, len));
-  SPSS_TRY(f64_set_natural_frequencies(ctx, ctx->scratch_a.ptr));
+  SPSS_TRY(is_f64(ctx) ? f64_set_natural_frequencies(ctx, ctx->scratch_a.ptr)
+                       : fast_set_natural_frequencies(ctx, ctx->scratch_a.ptr));
   SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return SPSS_OK;
 }

@@ -280,6 +280,7 @@ int fast_evaluate(spss_ctx *ctx, int variant, const double *d_state, const doubl
 int fast_step(spss_ctx *ctx, int stepper, double t, double dt);
 int fast_steps(spss_ctx *ctx, int stepper, double t0, double dt, int nsteps);
 int fast_noise(spss_ctx *ctx, int stepper, unsigned long long step, double *d_out);
+int fast_set_natural_frequencies(spss_ctx *ctx, const double *d_freqs);
 int fast_complementary_force(spss_ctx *ctx, double *d_out);
 int fast_apply_pbc(spss_ctx *ctx);
 

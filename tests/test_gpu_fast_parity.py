@@ -159,3 +159,31 @@ def test_deterministic_and_noise_reproducible():
             ctx.steps(2, 0.0, 0.005, 30)
             outs.append(ctx.get_state())
     np.testing.assert_array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("stepper", [1, 2])
+def test_global_field_matches_fp64_oracle(stepper):
+    """Global polar order field (first order) with natural frequencies: one and
+    ten steps against the FP64 oracle on identical noise, within the one-step
+    tolerance (1e-5) and the 50-step tolerance (99.9 % within 1e-3)."""
+    n = 4096
+    p = params(1, n, sigma=1.5, alpha=0.3)
+    x0 = initial(1, n, 21)
+    nu = np.random.default_rng(4).normal(0.0, 0.5, n)
+    ctx = gpu_context(p, precision=F32, variant=5, seed=13)
+    orc = oracle_system(p)
+    ctx.set_natural_frequencies(nu)
+    orc.set_natural_frequencies(nu)
+    ctx.set_state(x0)
+    x, t, dt = x0.copy(), 0.0, 0.005
+    for k in range(10):
+        t += dt
+        normals = ctx.noise(stepper, k)
+        ctx.step(stepper, t, dt)
+        orc.step(stepper, 5, x, t, dt, normals)
+        if k == 0:
+            assert state_err(ctx.get_state(), x, 4).max() <= 1e-5
+    err = state_err(ctx.get_state(), x, 4).max(axis=1)
+    ctx.close()
+    assert np.quantile(err, 0.999) <= 1e-3
+    assert np.median(err) <= 1e-5
