@@ -145,6 +145,20 @@ int spss_frame_async(spss_ctx *ctx, int mode, float *dst, long len);
 /* Page-locked host memory for frames (cudaMallocHost / cudaFreeHost). */
 int spss_pinned_alloc(size_t bytes, void **out);
 int spss_pinned_free(void *p);
+/* Adaptive integration with dense output, the reference's odeint path
+ * (SimulationEngineFirstOrder.cpp:158-165: integrate_const with
+ * make_dense_output(eps_abs, eps_rel, runge_kutta_dopri5) over the system's
+ * operator(), ParticleSystemFirstOrder.cpp:114-120): Dormand-Prince 5(4) over
+ * the FP64 right-hand side of the context's variant, the error norm and
+ * step-size rule of odeint's documented defaults, the continuous extension of
+ * Hairer, Norsett & Wanner for the observer times t0, t0 + dt_out, ... <= t1.
+ * The observer (may be NULL) receives the host state at each of those times and
+ * returns nonzero to stop.  The context's state ends at the last observer time
+ * (or, when stopped, at the last accepted step).  *steps (may be NULL) receives
+ * the number of accepted steps.  SPSS_PRECISION_F64 contexts. */
+typedef int (*spss_observer_fn)(const double *state, long len, double t, void *user);
+int spss_integrate_dopri5(spss_ctx *ctx, double t0, double t1, double dt_out, double eps_abs, double eps_rel,
+                          spss_observer_fn observer, void *user, long *steps);
 /* AveragingObserver::operator() and the averaged state (AveragingObserver.cpp:29-69). */
 int spss_average_accumulate(spss_ctx *ctx);
 int spss_average_get(spss_ctx *ctx, double *mean_state, long len, int *count);

@@ -102,6 +102,7 @@ SIGNATURES = {
     "spss_get_tiling": (_i, [_vp, _ip, _ip]),
     "spss_autotune": (_i, [_vp, _i, _d, _i, _dp]),
     "spss_frame_async": (_i, [_vp, _i, _fp, _l]),
+    "spss_integrate_dopri5": (_i, [_vp, _d, _d, _d, _d, _d, _vp, _vp, P(_l)]),
     "spss_pinned_alloc": (_i, [ctypes.c_size_t, P(_vp)]),
     "spss_pinned_free": (_i, [_vp]),
     # learned surrogate (include/spss_surrogate.h)
@@ -119,6 +120,10 @@ SIGNATURES = {
 MLP_INPUTS, MLP_HIDDEN, MLP_OUTPUTS, MLP_PARAMS = 5, 128, 4, 34308
 
 STATS_PER_SYSTEM = 5
+
+# spss_observer_fn: int (*)(const double *state, long len, double t, void *user)
+OBSERVER_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.c_long, ctypes.c_double,
+                               ctypes.c_void_p)
 
 
 def lib(path=None):

@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
                  "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
 PER_FILE = {"f64_path.cu": ["--fmad=false"]}
-SOURCES = ["common.cu", "f64_path.cu", "fast_path.cu", "spss_gpu.cu", "surrogate.cu"]
+SOURCES = ["common.cu", "f64_path.cu", "fast_path.cu", "spss_gpu.cu", "surrogate.cu", "dopri5.cu"]
 
 
 def nvcc():

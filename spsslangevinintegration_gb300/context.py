@@ -193,6 +193,24 @@ class Context:
         N.check(self.L.spss_kernel_launches(self.h, ctypes.byref(c)), "spss_kernel_launches")
         return c.value
 
+    # -- adaptive integration (FP64 contexts)
+    def integrate_dopri5(self, t0, t1, dt_out, eps_abs=1e-6, eps_rel=1e-6, observer=None):
+        """Dormand-Prince 5(4) with dense output from t0 to t1 (the reference's
+        odeint path); `observer(state, t)` is called at t0, t0 + dt_out, ...
+        with a copy of the host state and may return True to stop.  Returns
+        the number of accepted steps."""
+        def cb(ptr, n, t, user):
+            if observer is None:
+                return 0
+            return 1 if observer(np.ctypeslib.as_array(ptr, shape=(n,)).copy(), t) else 0
+
+        fn = N.OBSERVER_FN(cb)
+        steps = ctypes.c_long()
+        N.check(self.L.spss_integrate_dopri5(self.h, t0, t1, dt_out, eps_abs, eps_rel,
+                                             ctypes.cast(fn, ctypes.c_void_p), None, ctypes.byref(steps)),
+                "spss_integrate_dopri5")
+        return steps.value
+
     # -- tiling of the pair-and-update kernel (F32 contexts)
     def set_tiling(self, tile_cells, persistent=False):
         N.check(self.L.spss_set_tiling(self.h, int(tile_cells), int(bool(persistent))), "spss_set_tiling")
