@@ -893,6 +893,9 @@ __device__ __forceinline__ void candidate_staged(const FastParams &P, const uint
                                                  const uint4 *srec, const uint4 *saux, int idx, Acc &a)
 {
   const uint4 rj = srec[idx];
+  // the omega word is loaded with the record, before the range test, so the
+  // two shared-memory loads overlap instead of forming a dependent chain
+  const float wj = OMEGA ? __uint_as_float(saux[idx].w) : 0.0f;
   const float dx = (float) (int) (rj.x - ri.x);
   const float dy = (float) (int) (rj.y - ri.y);
   const float d2 = fmaf(dx, dx, dy * dy);
@@ -903,7 +906,7 @@ __device__ __forceinline__ void candidate_staged(const FastParams &P, const uint
     in = OUTLINE ? exact_within(rj.x, rj.y, l.x, l.y, Xi, Yi, P.rho2_d)
                  : exact_within_inline(rj.x, rj.y, l.x, l.y, Xi, Yi, P.rho2_d);
   }
-  if (in) accumulate(a, rj, OMEGA ? __uint_as_float(saux[idx].w) : 0.0f);
+  if (in) accumulate(a, rj, wj);
 }
 
 // Neighbour sums of slot q from the tile's staged records.
@@ -1324,8 +1327,6 @@ __global__ void __launch_bounds__(kTileThreads, 9) fast_tile_kernel(FastParams P
     const uint4 ai = ain[q];
     const int cnt = KIND == KIND_VERLET ? B.vl_cnt[q] : 0;
     const float2 v = MODEL == 2 ? B.vel[q] : make_float2(0.f, 0.f);
-    float z[6];
-    draw_noise<MODEL, STEPPER>(Q, ctrl->step, p, z);
     Acc a{0.f, 0.f, 0.f, 0.f, 0};
     const uint64_t Xi = join64(ri.x, ai.x), Yi = join64(ri.y, ai.y);
     const int i = q - L.p_begin;
@@ -1340,6 +1341,8 @@ __global__ void __launch_bounds__(kTileThreads, 9) fast_tile_kernel(FastParams P
                                              use_runs ? runs : nullptr, col_of, self_base);
     else
       gather_sums<KIND, STEPPER == 2>(Q, B, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
+    float z[6];
+    draw_noise<MODEL, STEPPER>(Q, ctrl->step, p, z);
     d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, ri, ai, v, a, z, rout, aout, err));
   }
   publish_max(ctrl, B.sysctl, sys, d2max, err);
