@@ -993,13 +993,13 @@ __device__ __forceinline__ void draw_noise(const FastParams &P, unsigned long lo
   nk.step = step;
   p -= (unsigned) P.first;  // index of the particle within its system
   const uint4 u = philox_block(nk, p, 0);
-  box_muller_f32(u.x, u.y, z[0], z[1]);
-  if (kNeed > 2) box_muller_f32(u.z, u.w, z[2], z[3]);
   if (kNeed > 4)
   {
-    const uint4 u1 = philox_block(nk, p, 1);
-    box_muller_f32(u1.x, u1.y, z[4], z[5]);
+    box_muller6_f32(u, z);  // six normals from the one block
+    return;
   }
+  box_muller_f32(u.x, u.y, z[0], z[1]);
+  if (kNeed > 2) box_muller_f32(u.z, u.w, z[2], z[3]);
 }
 
 // Torque derivative f_w and (SRK) complementary force C from the neighbour
@@ -1478,9 +1478,14 @@ __global__ void fast_noise_kernel(double *__restrict__ out, int n, int per, Nois
   const SysParams *S = sys + sys_of[p];
   nk.replica = (uint32_t) S->replica;
   const uint32_t local = (uint32_t) (p - S->first);
-  float z[8];
-  normals4_f32(nk, local, 0, z);
-  if (per > 4) normals4_f32(nk, local, 1, z + 4);
+  float z[6];
+  if (per > 4)
+  {
+    box_muller6_f32(philox_block(nk, local, 0), z);
+  } else
+  {
+    normals4_f32(nk, local, 0, z);
+  }
   for (int d = 0; d < per; ++d) out[(long) per * p + d] = (double) z[d];
 }
 

@@ -111,6 +111,29 @@ __device__ __forceinline__ void box_muller_f32(uint32_t a, uint32_t b, float &z0
   z1 = __fmul_rn(r, s);
 }
 
+// Six normals from one Philox block (128 bits), for the steps that need six
+// (second-order SRK): three Box-Muller pairs with 24-bit radius uniforms (the
+// top 24 bits of words 0..2) and 16-bit angle uniforms (the two halves of
+// word 3, and the low bytes of words 0 and 1).  A 16-bit angle is resolved to
+// 1e-4 rad; the radius keeps the tails of the 24-bit draws above.
+__device__ __forceinline__ void box_muller6_f32(const uint4 &u, float z[6])
+{
+  const uint32_t a[3] = {u.x >> 8, u.y >> 8, u.z >> 8};
+  const uint32_t b[3] = {u.w & 0xffffu, u.w >> 16, (u.x & 0xffu) | ((u.y & 0xffu) << 8)};
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+  {
+    const float u1 = __fmul_rn(__fadd_rn((float) a[k], 0.5f), 5.9604644775390625e-8f);
+    const float theta = __fmul_rn(__fadd_rn(__fmul_rn(__fadd_rn((float) b[k], 0.5f), 1.52587890625e-5f), -0.5f),
+                                  6.2831853f);
+    const float r = sqrtf(__fmul_rn(-2.0f, __logf(u1)));
+    float s, c;
+    __sincosf(theta, &s, &c);
+    z[2 * k] = __fmul_rn(r, c);
+    z[2 * k + 1] = __fmul_rn(r, s);
+  }
+}
+
 // Normal number d (0-based, reference draw order) of one particle at one step.
 __device__ __forceinline__ double normal_f64(const NoiseKey &nk, uint32_t particle, int d)
 {

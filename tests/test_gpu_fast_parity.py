@@ -161,6 +161,28 @@ def test_deterministic_and_noise_reproducible():
     np.testing.assert_array_equal(outs[0], outs[1])
 
 
+@pytest.mark.parametrize("model,stepper,per", [(2, 2, 6), (2, 1, 3), (1, 2, 2), (1, 1, 1)])
+def test_fast_noise_is_standard_normal_and_independent(model, stepper, per):
+    """The fast path's normals (six from one Philox block for second-order SRK,
+    Box-Muller pairs otherwise): mean, variance, kurtosis, tail mass, and no
+    correlation between a particle's components or their squares."""
+    n = 200000
+    p = params(model, n)
+    r_max = 1.3 * p["rho"]
+    with gpu_context(p, precision=F32, variant=4, r_max=r_max, nc_verlet=int(1 / r_max), seed=5) as ctx:
+        z = np.concatenate([ctx.noise(stepper, k).reshape(n, per) for k in range(3)])
+    m = z.shape[0]
+    assert np.abs(z.mean(axis=0)).max() < 5 * np.sqrt(1.0 / m)
+    assert np.abs(z.var(axis=0) - 1.0).max() < 5 * np.sqrt(2.0 / m)
+    assert np.abs((z ** 4).mean(axis=0) - 3.0).max() < 5 * np.sqrt(96.0 / m)
+    tail = (np.abs(z) > 3.0).mean(axis=0)  # 2.6998e-3 for a standard normal
+    assert np.abs(tail - 2.6998e-3).max() < 5 * np.sqrt(2.7e-3 / m)
+    if per > 1:
+        off = ~np.eye(per, dtype=bool)
+        assert np.abs(np.corrcoef(z.T)[off]).max() < 5 / np.sqrt(m)
+        assert np.abs(np.corrcoef((z ** 2).T)[off]).max() < 5 / np.sqrt(m)
+
+
 @pytest.mark.parametrize("stepper", [1, 2])
 def test_global_field_matches_fp64_oracle(stepper):
     """Global polar order field (first order) with natural frequencies: one and
