@@ -1198,33 +1198,59 @@ __device__ __forceinline__ uint32_t wait_phase(uint32_t mb, uint32_t phase)
   return done;
 }
 
-// The particles of one tile, one per thread.
+// A particle's own words, loaded from global memory at its slot.
+struct OwnParticle
+{
+  unsigned p;  // original index (noise counter)
+  uint4 r, a;  // record and aux words
+  int cnt;     // Verlet list length
+  float2 v;    // velocity (second order)
+};
+
+template<int MODEL, int KIND>
+__device__ __forceinline__ OwnParticle load_own(const FastBuffers &B, const uint4 *rin, const uint4 *ain, int q)
+{
+  OwnParticle o;
+  o.p = B.pid[q];
+  o.r = rin[q];
+  o.a = ain[q];
+  o.cnt = KIND == KIND_VERLET ? B.vl_cnt[q] : 0;
+  o.v = MODEL == 2 ? B.vel[q] : make_float2(0.f, 0.f);
+  return o;
+}
+
+// The particles of one tile, one per thread; `o` holds the thread's first
+// particle, loaded before the wait for the tile's bulk copies.  The noise is
+// drawn after the neighbour walk (fewer registers live across the walk).
 template<int MODEL, int STEPPER, int KIND>
 __device__ __forceinline__ void step_tile(const FastParams &Q, const FastBuffers &B, const TileLayout &L,
-                                          const uint4 *srec, const uint4 *saux, const short *slist, const short *glist,
-                                          int list_staged, int list_stride, bool staged, const uint4 *rin,
-                                          const uint4 *ain, uint4 *rout, uint4 *aout, float &d2max, int &err,
-                                          const StencilRuns *runs, const unsigned char *col_of, int self_base)
+                                          OwnParticle o, const uint4 *srec, const uint4 *saux, const short *slist,
+                                          const short *glist, int list_staged, int list_stride, bool staged,
+                                          const uint4 *rin, const uint4 *ain, uint4 *rout, uint4 *aout, float &d2max,
+                                          int &err, const StencilRuns *runs, const unsigned char *col_of,
+                                          int self_base)
 {
-  for (int q = L.p_begin + threadIdx.x; q < L.p_end; q += blockDim.x)
+  const int q0 = L.p_begin + threadIdx.x;
+  for (int q = q0; q < L.p_end; q += blockDim.x)
   {
-    const unsigned p = B.pid[q];
-    const uint4 ri = rin[q];
-    const uint4 ai = ain[q];
-    const int cnt = KIND == KIND_VERLET ? B.vl_cnt[q] : 0;
-    const float2 v = MODEL == 2 ? B.vel[q] : make_float2(0.f, 0.f);
-    float z[6];
-    draw_noise<MODEL, STEPPER>(Q, B.ctrl->step, p, z);
+    if (q != q0) o = load_own<MODEL, KIND>(B, rin, ain, q);
     Acc a{0.f, 0.f, 0.f, 0.f, 0};
-    const uint64_t Xi = join64(ri.x, ai.x), Yi = join64(ri.y, ai.y);
+    const uint64_t Xi = join64(o.r.x, o.a.x), Yi = join64(o.r.y, o.a.y);
     const int i = q - L.p_begin;
     const short *lp = KIND == KIND_VERLET ? (list_staged ? slist + i : glist + i) : nullptr;
-    if (staged)
-      gather_sums_staged<KIND, STEPPER == 2>(Q, B, srec, saux, L, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a,
-                                             runs, col_of, self_base);
+    // a staged list is walked through its shared-memory pointer, so its
+    // entries are read with shared-memory loads
+    if (staged && KIND == KIND_VERLET && list_staged)
+      gather_sums_staged<KIND, STEPPER == 2>(Q, B, srec, saux, L, rin, ain, q, o.cnt, slist + i, list_stride, o.r,
+                                             Xi, Yi, a, nullptr, col_of, self_base);
+    else if (staged)
+      gather_sums_staged<KIND, STEPPER == 2>(Q, B, srec, saux, L, rin, ain, q, o.cnt, lp, list_stride, o.r, Xi, Yi,
+                                             a, runs, col_of, self_base);
     else
-      gather_sums<KIND, STEPPER == 2>(Q, B, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
-    d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, ri, ai, v, a, z, rout, aout, err));
+      gather_sums<KIND, STEPPER == 2>(Q, B, rin, ain, q, o.cnt, lp, list_stride, o.r, Xi, Yi, a);
+    float z[6];
+    draw_noise<MODEL, STEPPER>(Q, B.ctrl->step, o.p, z);
+    d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, o.r, o.a, o.v, a, z, rout, aout, err));
   }
 }
 
@@ -1306,6 +1332,11 @@ __global__ void __launch_bounds__(kTileThreads, 9) fast_tile_kernel(FastParams P
   const bool use_runs = KIND == KIND_CELLS && staged && L.ncols <= kRunCells;
   if (use_runs) build_runs(L, B.cell_off + Q.cell0, Q.nc, runs, col_of, &self_base, &ctrl->error);
   const short *glist = KIND == KIND_VERLET ? B.vl + tile_list_base(P.cap, t, L.p_begin) : nullptr;
+  // the thread's first particle is loaded before the wait for the bulk
+  // copies, so its global loads are in flight while the tile lands
+  const int q0 = L.p_begin + threadIdx.x;
+  OwnParticle o;
+  if (q0 < L.p_end) o = load_own<MODEL, KIND>(B, rin, ain, q0);
   if (staged)
   {
     const uint32_t done = wait_phase(mb, 0);
@@ -1320,13 +1351,16 @@ __global__ void __launch_bounds__(kTileThreads, 9) fast_tile_kernel(FastParams P
   }
   float d2max = 0.0f;
   int err = 0;
-  for (int q = L.p_begin + threadIdx.x; q < L.p_end; q += blockDim.x)
+  // the loop body is step_tile's, written out here: through the shared
+  // function this kernel spills and runs 1 % slower
+  for (int q = q0; q < L.p_end; q += blockDim.x)
   {
-    const unsigned p = B.pid[q];
-    const uint4 ri = rin[q];
-    const uint4 ai = ain[q];
-    const int cnt = KIND == KIND_VERLET ? B.vl_cnt[q] : 0;
-    const float2 v = MODEL == 2 ? B.vel[q] : make_float2(0.f, 0.f);
+    if (q != q0) o = load_own<MODEL, KIND>(B, rin, ain, q);
+    const unsigned p = o.p;
+    const uint4 ri = o.r;
+    const uint4 ai = o.a;
+    const int cnt = o.cnt;
+    const float2 v = o.v;
     Acc a{0.f, 0.f, 0.f, 0.f, 0};
     const uint64_t Xi = join64(ri.x, ai.x), Yi = join64(ri.y, ai.y);
     const int i = q - L.p_begin;
@@ -1402,6 +1436,8 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_persistent_kernel(F
         build_runs(L, B.cell_off + P.cell0, P.nc, runs, col_of, &self_base, &ctrl->error);
       }
     }
+    OwnParticle o;
+    if (L.p_begin + (int) threadIdx.x < L.p_end) o = load_own<MODEL, KIND>(B, rin, ain, L.p_begin + threadIdx.x);
     if (staged)
     {
       const uint32_t ph = phase;
@@ -1419,10 +1455,10 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_persistent_kernel(F
     float d2max = 0.0f;
     int err = 0;
     if (!MULTI)
-      step_tile<MODEL, STEPPER, KIND>(P, B, L, srec, saux, slist, glist, list_staged, list_stride, staged, rin, ain,
-                                      rout, aout, d2max, err, use_runs ? runs : nullptr, col_of, self_base);
+      step_tile<MODEL, STEPPER, KIND>(P, B, L, o, srec, saux, slist, glist, list_staged, list_stride, staged, rin,
+                                      ain, rout, aout, d2max, err, use_runs ? runs : nullptr, col_of, self_base);
     else
-      step_tile<MODEL, STEPPER, KIND>(with_system(P, B.sys[sys]), B, L, srec, saux, slist, glist, list_staged,
+      step_tile<MODEL, STEPPER, KIND>(with_system(P, B.sys[sys]), B, L, o, srec, saux, slist, glist, list_staged,
                                       list_stride, staged, rin, ain, rout, aout, d2max, err,
                                       use_runs ? runs : nullptr, col_of, self_base);
     publish_max(ctrl, B.sysctl, sys, d2max, err);
