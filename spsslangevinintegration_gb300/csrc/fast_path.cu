@@ -246,18 +246,12 @@ __device__ __forceinline__ FastParams with_system(const FastParams &P, const Sys
 // mantissa; |f| < 0.5 (one step never moves a particle half a box).
 __device__ __forceinline__ long long fix64_of(float f, int &err)
 {
-  const uint32_t b = __float_as_uint(f);
-  const int e = (int) ((b >> 23) & 0xffu);
-  if (e == 0) return 0;
-  if (e >= 126)
+  if (!(fabsf(f) < 0.5f))
   {
     err = 1;
     return 0;
   }
-  const long long m = (long long) ((b & 0x7fffffu) | 0x800000u);
-  const int sh = e - 86;
-  long long v = sh >= 0 ? (m << sh) : (sh > -24 ? (m >> (-sh)) : 0);
-  return (b >> 31) ? -v : v;
+  return __float2ll_rz(__fmul_rn(f, 18446744073709551616.0f));  // exact scaling by 2^64, then truncation
 }
 
 // X += dX on the periodic unit box; `carry` receives the box crossing (-1, 0, 1).
@@ -284,9 +278,32 @@ __device__ __forceinline__ uint32_t advance_phase(uint32_t P, float dphi, int &c
   return R;
 }
 
+// sin and cos of the fixed-point phase P (one turn = 2^32).  The nearest
+// quarter turn comes exactly from the top bits; the remainder is the angle
+// theta = 2 pi r 2^-32 in [-pi/4, pi/4), where sin and cos are an odd degree-7
+// and an even degree-8 polynomial in theta (coefficients fitted by weighted
+// least squares on Chebyshev nodes of theta^2, rounded to float).  The
+// result is within 1e-7 of the exact sin and cos of the phase over all 2^32
+// phases (the rounding of theta to float is the larger part); the quarter-turn
+// rotation is exact.  Rounding is spelled out so every copy gives the same bits.
 __device__ __forceinline__ void phase_sincos(uint32_t P, float &s, float &c)
 {
-  sincospif((float) (int) P * 4.656612873077393e-10f, &s, &c);  // P * 2^-31 in [-1, 1)
+  const uint32_t qd = (P + 0x20000000u) >> 30;  // nearest quarter turn (mod 4)
+  const int r = (int) (P - (qd << 30));         // [-2^29, 2^29)
+  const float th = __fmul_rn((float) r, 1.4629180792671596e-9f);  // 2 pi / 2^32
+  const float t2 = __fmul_rn(th, th);
+  const float ps = fmaf(th, __fmul_rn(t2, fmaf(t2, fmaf(t2, -1.9520212663337588e-4f, 8.332204073667526e-3f),
+                                               -0.16666655242443085f)),
+                        th);
+  const float pc = fmaf(t2, fmaf(t2, fmaf(t2, fmaf(t2, 2.4394103093072772e-5f, -1.3886808883398771e-3f),
+                                          4.166662320494652e-2f),
+                                 -0.5f),
+                        1.0f);
+  // rotate by qd quarter turns: (sin, cos) = (ps, pc), (pc, -ps), (-ps, -pc), (-pc, ps)
+  const float a = (qd & 1u) ? pc : ps;
+  const float b = (qd & 1u) ? ps : pc;
+  s = (qd & 2u) ? -a : a;
+  c = ((qd + 1u) & 2u) ? -b : b;
 }
 
 __device__ __forceinline__ int cell_of_fix(uint64_t X, uint64_t Y, int nc)
