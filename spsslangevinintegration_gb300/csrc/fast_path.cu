@@ -787,11 +787,11 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p)
 // slot q at vl[m * n + q] (16 bits): the neighbour's shared-memory index when
 // q's tile is staged, else the offset j - q.  A count of -1 marks a list
 // longer than the capacity or an offset beyond 16 bits; the step then scans
-// the stencil of the rebuild-time cell instead.
-__global__ void fast_verlet_build_kernel(FastParams P, FastBuffers B)
+// the stencil of the rebuild-time cell instead.  This per-slot form (global
+// gathers) serves the tiles whose neighbourhood is not staged; the staged
+// tiles build in fast_verlet_tile_build_kernel.
+__device__ void verlet_build_slot(const FastParams &P, const FastBuffers &B, int q)
 {
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= P.n) return;
   const int par = B.ctrl->parity;
   const uint4 *rec = par ? B.rec1 : B.rec0;
   const uint4 ri = rec[q];
@@ -1480,6 +1480,108 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_persistent_kernel(F
                                       use_runs ? runs : nullptr, col_of, self_base);
     publish_max(ctrl, B.sysctl, sys, d2max, err);
   }
+}
+
+// Verlet lists of one tile per CTA, from the 3x3 stencil of the rebuild grid
+// (ParticleSystemFirstOrder.cpp:536-589).  The tile's neighbourhood records
+// are staged in shared memory by bulk copies; each particle scans its stencil
+// through the tile's run table (per stencil row at most three contiguous runs
+// of staged records, in the reference's stencil order), so its list holds the
+// same entries, in the same order, as the per-slot build: the staged indices
+// of the neighbours with r <= r_max (widened by the guard band).  Tiles that
+// are not staged, or wider than the run table, build per slot from global
+// memory.  The entries go straight to global memory (L2 merges the 2-byte
+// stores; assembling the rows in shared memory first measured slower).  The
+// tile's longest list (rows to stage at the step) is a block maximum.
+__global__ void __launch_bounds__(kTileThreads) fast_verlet_tile_build_kernel(FastParams P, FastBuffers B)
+{
+  __shared__ __align__(16) uint4 srec[kTileCap];
+  __shared__ __align__(8) unsigned long long mbar;
+  __shared__ TileLayout L;
+  __shared__ int self_base, tile_max;
+  __shared__ StencilRuns runs[kRunCells];
+  __shared__ unsigned char col_of[kTileCap];
+  FastControl *ctrl = B.ctrl;
+  const int t = blockIdx.x;
+  const uint4 *rec = ctrl->parity ? B.rec1 : B.rec0;
+  const SysParams *S = B.sys + B.tile_sys[t];
+  const uint32_t mb = smem_u32(&mbar);
+  if (threadIdx.x == 0)
+  {
+    tile_max = 0;
+    L = reinterpret_cast<const TileLayout *>(B.tiles)[t];
+    if (L.p_end <= L.p_begin || L.ncols > kRunCells) L.staged = 0;
+    if (L.staged)
+    {
+      init_mbarrier(mb);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(16u * L.total) : "memory");
+      for (int k = 0; k < L.nseg; ++k)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(&srec[L.base[k]])),
+                     "l"(rec + L.start[k]), "r"(16u * L.len[k]), "r"(mb)
+                     : "memory");
+    }
+  }
+  __syncthreads();
+  if (L.p_end <= L.p_begin) return;
+  if (!L.staged)
+  {
+    for (int q = L.p_begin + threadIdx.x; q < L.p_end; q += blockDim.x) verlet_build_slot(P, B, q);
+    return;
+  }
+  build_runs(L, B.cell_off + S->cell0, S->nc, runs, col_of, &self_base, &ctrl->error);
+  const uint32_t done = wait_phase(mb, 0);
+  if (!__syncthreads_and(done))
+  {
+    // the copies did not complete in time: report, wait once more so none is
+    // in flight when the CTA exits, and leave the lists unbuilt
+    if (threadIdx.x == 0) atomicOr(&ctrl->error, 2);
+    wait_phase(mb, 0);
+    return;
+  }
+  const float rmax2 = S->rmax2_f;
+  const int stride = tile_list_stride(L.p_begin, L.p_end);
+  short *const rows = B.vl + tile_list_base(P.cap, t, L.p_begin);
+  int mymax = 0;
+  for (int q = L.p_begin + threadIdx.x; q < L.p_end; q += blockDim.x)
+  {
+    const int i = q - L.p_begin;
+    const int self = q + self_base;
+    const uint4 ri = srec[self];
+    const StencilRuns &R = runs[col_of[i]];
+    int off = i;  // entry cnt of this particle at off = i + cnt * stride
+    int cnt = 0;
+#pragma unroll 1
+    for (int r = 0; r < 3; ++r)
+#pragma unroll 1
+      for (int u = 0; u < 3; ++u)
+      {
+        const int e = R.e[r][u];
+        for (int idx = R.s[r][u]; idx < e; ++idx)
+        {
+          const uint4 rj = srec[idx];
+          const float dx = (float) (int) (rj.x - ri.x);
+          const float dy = (float) (int) (rj.y - ri.y);
+          if (idx != self && fmaf(dx, dx, dy * dy) <= rmax2)
+          {
+            if (cnt < P.cap)
+            {
+              rows[off] = (short) idx;
+              off += stride;
+            }
+            ++cnt;
+          }
+        }
+      }
+    if (cnt > P.cap) atomicMax(&ctrl->overflow, cnt);
+    B.vl_cnt[q] = cnt > P.cap ? -1 : cnt;
+    mymax = max(mymax, min(cnt, P.cap));
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) mymax = max(mymax, __shfl_xor_sync(0xffffffffu, mymax, off));
+  if ((threadIdx.x & 31) == 0) atomicMax(&tile_max, mymax);
+  __syncthreads();
+  if (threadIdx.x == 0) B.tile_maxcnt[t] = tile_max;
 }
 
 // After a step: advance the noise counter and the buffer parity, accumulate
@@ -2193,9 +2295,9 @@ static int launch_rebuild(spss_ctx *ctx, const FastParams &P)
   if (f->kind == KIND_VERLET)
   {
     SPSS_CUDA_TRY(cudaMemsetAsync(f->tile_maxcnt.ptr, 0, sizeof(int) * f->tile_maxcnt.count, ctx->stream));
-    fast_verlet_build_kernel<<<blocks_for(n, 128), 128, 0, ctx->stream>>>(P, buffers(ctx));
+    fast_verlet_tile_build_kernel<<<f->ntiles, kTileThreads, 0, ctx->stream>>>(P, buffers(ctx));
     ++ctx->launches;
-    SPSS_TRY(check_launch("fast_verlet_build_kernel"));
+    SPSS_TRY(check_launch("fast_verlet_tile_build_kernel"));
   }
   return SPSS_OK;
 }
