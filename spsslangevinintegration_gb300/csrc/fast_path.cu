@@ -100,6 +100,7 @@ struct FastParams
   float dt, sqdt, half_dt2, half_dt15, inv_sqrt3, b_r, b_phi;
   uint64_t seed;
   uint32_t replica;
+  uint32_t kx[10], ky[10];  // Philox round keys of `seed`, the same for every particle
 };
 
 struct FastBuffers
@@ -1004,12 +1005,9 @@ template<int MODEL, int STEPPER>
 __device__ __forceinline__ void draw_noise(const FastParams &P, unsigned long long step, unsigned p, float z[6])
 {
   constexpr int kNeed = MODEL == 1 ? (STEPPER == 1 ? 1 : 2) : (STEPPER == 1 ? 3 : 6);
-  NoiseKey nk;
-  nk.seed = P.seed;
-  nk.replica = P.replica;
-  nk.step = step;
   p -= (unsigned) P.first;  // index of the particle within its system
-  const uint4 u = philox_block(nk, p, 0);
+  // philox_block(seed, replica, step; p, block 0) with the round keys from the parameters
+  const uint4 u = philox_keyed(make_uint4(p, (uint32_t) step, (uint32_t) (step >> 32), P.replica << 8), P.kx, P.ky);
   if (kNeed > 4)
   {
     box_muller6_f32(u, z);  // six normals from the one block
@@ -2018,6 +2016,7 @@ static FastParams params(spss_ctx *ctx, double dt)
   P.half_dt15 = (float) (0.5 * std::pow(dt, 1.5));
   P.inv_sqrt3 = (float) (1.0 / std::sqrt(3.0));
   P.seed = p.seed;
+  philox_round_keys(p.seed, P.kx, P.ky);
   P.replica = (uint32_t) S.replica;
   return P;
 }

@@ -64,6 +64,36 @@ struct Philox
   }
 };
 
+// The ten round keys of a seed (the Weyl sequence of Philox4x32-10).
+__host__ __device__ inline void philox_round_keys(uint64_t seed, uint32_t kx[10], uint32_t ky[10])
+{
+  uint32_t a = (uint32_t) seed, b = (uint32_t) (seed >> 32);
+  for (int r = 0; r < 10; ++r)
+  {
+    kx[r] = a;
+    ky[r] = b;
+    a += 0x9E3779B9u;
+    b += 0xBB67AE85u;
+  }
+}
+
+// Philox4x32-10 with the round keys given (equal to Philox::generate with
+// the seed they come from), so a kernel takes them from its parameters
+// instead of recomputing the key schedule per draw.
+__device__ __forceinline__ uint4 philox_keyed(uint4 c, const uint32_t kx[10], const uint32_t ky[10])
+{
+#pragma unroll
+  for (int r = 0; r < 10; ++r)
+  {
+    const uint64_t p0 = (uint64_t) 0xD2511F53u * c.x;
+    const uint64_t p1 = (uint64_t) 0xCD9E8D57u * c.z;
+    const uint32_t hi0 = (uint32_t) (p0 >> 32), lo0 = (uint32_t) p0;
+    const uint32_t hi1 = (uint32_t) (p1 >> 32), lo1 = (uint32_t) p1;
+    c = make_uint4(hi1 ^ c.y ^ kx[r], lo1, hi0 ^ c.w ^ ky[r], lo0);
+  }
+  return c;
+}
+
 struct NoiseKey
 {
   uint64_t seed;
