@@ -904,11 +904,30 @@ __device__ __forceinline__ void gather_sums(const FastParams &P, const FastBuffe
   }
 }
 
+// The FP64 cutoff decision for a staged candidate inside the guard band when
+// the aux words are not staged (steppers that need no neighbour omega): the
+// low position words come from global memory at the candidate's slot.
+__device__ __forceinline__ bool exact_within_slot_inline(const TileLayout &L, const uint4 *__restrict__ aux, int idx,
+                                                        uint32_t xh, uint32_t yh, uint64_t Xi, uint64_t Yi,
+                                                        double rho2)
+{
+  const uint2 l = __ldg(reinterpret_cast<const uint2 *>(&aux[staged_slot(L, idx)]));
+  return exact_within_inline(xh, yh, l.x, l.y, Xi, Yi, rho2);
+}
+
+__device__ __noinline__ bool exact_within_slot(const TileLayout &L, const uint4 *__restrict__ aux, int idx,
+                                               uint32_t xh, uint32_t yh, uint64_t Xi, uint64_t Yi, double rho2)
+{
+  return exact_within_slot_inline(L, aux, idx, xh, yh, Xi, Yi, rho2);
+}
+
 // One staged candidate: the record comes from shared memory; the guard band
-// (rare) still reads the slot's low position words from global memory.
+// (rare) takes the slot's low position words from the staged aux words (SRK,
+// which stages them for the neighbours' omega) or from global memory (SE).
 template<bool OMEGA, bool OUTLINE = true>
 __device__ __forceinline__ void candidate_staged(const FastParams &P, const uint4 &ri, uint64_t Xi, uint64_t Yi,
-                                                 const uint4 *srec, const uint4 *saux, int idx, Acc &a)
+                                                 const uint4 *srec, const uint4 *saux, const TileLayout &L,
+                                                 const uint4 *__restrict__ aux, int idx, Acc &a)
 {
   const uint4 rj = srec[idx];
   // the omega word is loaded with the record, before the range test, so the
@@ -920,9 +939,16 @@ __device__ __forceinline__ void candidate_staged(const FastParams &P, const uint
   bool in = d2 <= P.rho2_f;
   if (fabsf(d2 - P.rho2_f) <= P.band_f)
   {
-    const uint4 l = saux[idx];
-    in = OUTLINE ? exact_within(rj.x, rj.y, l.x, l.y, Xi, Yi, P.rho2_d)
-                 : exact_within_inline(rj.x, rj.y, l.x, l.y, Xi, Yi, P.rho2_d);
+    if (OMEGA)
+    {
+      const uint4 l = saux[idx];
+      in = OUTLINE ? exact_within(rj.x, rj.y, l.x, l.y, Xi, Yi, P.rho2_d)
+                   : exact_within_inline(rj.x, rj.y, l.x, l.y, Xi, Yi, P.rho2_d);
+    } else
+    {
+      in = OUTLINE ? exact_within_slot(L, aux, idx, rj.x, rj.y, Xi, Yi, P.rho2_d)
+                   : exact_within_slot_inline(L, aux, idx, rj.x, rj.y, Xi, Yi, P.rho2_d);
+    }
   }
   if (in) accumulate(a, rj, wj);
 }
@@ -948,7 +974,7 @@ __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const Fa
       {
         const int e = R.e[r][u];
         for (int idx = R.s[r][u]; idx < e; ++idx)
-          if (idx != self) candidate_staged<OMEGA, true>(P, ri, Xi, Yi, srec, saux, idx, a);
+          if (idx != self) candidate_staged<OMEGA, true>(P, ri, Xi, Yi, srec, saux, L, aux, idx, a);
       }
     return;
   }
@@ -960,14 +986,14 @@ __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const Fa
     {
       const int i0 = lp[0], i1 = lp[n], i2 = lp[2 * n], i3 = lp[3 * n];
       lp += 4 * n;
-      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, i0, a);
-      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, i1, a);
-      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, i2, a);
-      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, i3, a);
+      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, L, aux, i0, a);
+      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, L, aux, i1, a);
+      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, L, aux, i2, a);
+      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, L, aux, i3, a);
     }
     for (; m < cnt; ++m)
     {
-      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, lp[0], a);
+      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, L, aux, lp[0], a);
       lp += n;
     }
     return;
@@ -995,7 +1021,7 @@ __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const Fa
       }
       const int self = q - b;
       for (int u = 0; u < e - b; ++u)
-        if (u != self) candidate_staged<OMEGA, KIND == KIND_CELLS>(P, ri, Xi, Yi, srec, saux, i0 + u, a);
+        if (u != self) candidate_staged<OMEGA, KIND == KIND_CELLS>(P, ri, Xi, Yi, srec, saux, L, aux, i0 + u, a);
     }
   }
 }
@@ -1270,8 +1296,9 @@ __device__ __forceinline__ void step_tile(const FastParams &Q, const FastBuffers
 }
 
 // Staging of tile t by thread 0: layout, list geometry, and the bulk copies of
-// the neighbour records, aux words and list rows onto the mbarrier.
-template<int KIND>
+// the neighbour records, aux words (AUX: SRK, which needs the neighbours'
+// omega) and list rows onto the mbarrier.
+template<int KIND, bool AUX>
 __device__ __forceinline__ void stage_tile(const FastParams &P, const FastBuffers &B, int t, const uint4 *rin,
                                            const uint4 *ain, uint4 *srec, uint4 *saux, short *slist, uint32_t mb,
                                            TileLayout &L, int &list_staged, int &list_stride, bool reuse)
@@ -1285,18 +1312,19 @@ __device__ __forceinline__ void stage_tile(const FastParams &P, const FastBuffer
   if (!L.staged) return;
   // generic-proxy reads of the buffers (previous tile) before async-proxy writes
   if (reuse) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  const uint32_t tx = 32u * L.total + (list_staged ? list_bytes : 0u);
+  const uint32_t tx = (AUX ? 32u : 16u) * L.total + (list_staged ? list_bytes : 0u);
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(tx) : "memory");
   for (int k = 0; k < L.nseg; ++k)
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      smem_u32(&srec[L.base[k]])),
                  "l"(rin + L.start[k]), "r"(16u * L.len[k]), "r"(mb)
                  : "memory");
-  for (int k = 0; k < L.nseg; ++k)
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(&saux[L.base[k]])),
-                 "l"(ain + L.start[k]), "r"(16u * L.len[k]), "r"(mb)
-                 : "memory");
+  if (AUX)
+    for (int k = 0; k < L.nseg; ++k)
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                       smem_u32(&saux[L.base[k]])),
+                   "l"(ain + L.start[k]), "r"(16u * L.len[k]), "r"(mb)
+                   : "memory");
   if (list_staged)
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      smem_u32(slist)),
@@ -1314,11 +1342,14 @@ __device__ __forceinline__ void init_mbarrier(uint32_t mb)
 // memory by TMA bulk copies (cp.async.bulk, completion on an mbarrier).
 // MULTI: several systems, whose parameters come from the system table (one
 // system: from the kernel's parameter space, which costs no registers).
+// Residency: SRK 9 CTAs per SM (56 registers, 24.7 KB of shared memory); SE
+// stages no aux words (11 KB) and runs 14 CTAs per SM, which measured faster
+// than 9, 10 or 12 despite a few spilled registers.
 template<int MODEL, int STEPPER, int KIND, bool MULTI>
-__global__ void __launch_bounds__(kTileThreads, 9) fast_tile_kernel(FastParams P, FastBuffers B)
+__global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9 : 14) fast_tile_kernel(FastParams P, FastBuffers B)
 {
   __shared__ __align__(16) uint4 srec[kTileCap];
-  __shared__ __align__(16) uint4 saux[kTileCap];
+  __shared__ __align__(16) uint4 saux[STEPPER == 2 ? kTileCap : 1];  // aux words: SRK only (neighbour omega)
   __shared__ __align__(16) short slist[KIND == KIND_VERLET ? kListCap : 8];
   __shared__ __align__(8) unsigned long long mbar;
   __shared__ TileLayout L;
@@ -1336,7 +1367,7 @@ __global__ void __launch_bounds__(kTileThreads, 9) fast_tile_kernel(FastParams P
   if (threadIdx.x == 0)
   {
     init_mbarrier(mb);
-    stage_tile<KIND>(P, B, t, rin, ain, srec, saux, slist, mb, L, list_staged, list_stride, false);
+    stage_tile<KIND, STEPPER == 2>(P, B, t, rin, ain, srec, saux, slist, mb, L, list_staged, list_stride, false);
   }
   __syncthreads();
   const bool staged = L.staged;
@@ -1404,7 +1435,7 @@ template<int MODEL, int STEPPER, int KIND, bool MULTI>
 __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_persistent_kernel(FastParams P, FastBuffers B)
 {
   __shared__ __align__(16) uint4 srec[kTileCap];
-  __shared__ __align__(16) uint4 saux[kTileCap];
+  __shared__ __align__(16) uint4 saux[STEPPER == 2 ? kTileCap : 1];  // aux words: SRK only (neighbour omega)
   __shared__ __align__(16) short slist[KIND == KIND_VERLET ? kListCap : 8];
   __shared__ __align__(8) unsigned long long mbar;
   __shared__ TileLayout L;
@@ -1432,7 +1463,8 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_persistent_kernel(F
       const int t = atomicAdd(&ctrl->tile_next, 1);
       tile_id = t;
       if (t < P.ntiles)
-        stage_tile<KIND>(P, B, t, rin, ain, srec, saux, slist, mb, L, list_staged, list_stride, !first);
+        stage_tile<KIND, STEPPER == 2>(P, B, t, rin, ain, srec, saux, slist, mb, L, list_staged, list_stride,
+                                       !first);
     }
     __syncthreads();
     const int t = tile_id;
