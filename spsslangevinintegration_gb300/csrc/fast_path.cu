@@ -8,7 +8,10 @@
 //   aux[2][n]  uint4 {x_lo, y_lo, phase, omega}, double-buffered with rec
 //   vel[n]     float2 {v_x, v_y} (second-order model), updated in place
 //   pid[n]     original particle index (noise counter, output order); inv[n]
-//              its inverse; img[n] box crossings; turns[n] 2*pi turns of phase
+//              its inverse
+//   img[n], turns[n]  box crossings and 2*pi turns of the phase, indexed by
+//              original index (they change rarely, so the slot re-sort of a
+//              rebuild does not move them)
 // x = img + (x_hi * 2^32 + x_lo) * 2^-64 (unit box), phase = 2*pi*(turns + phase * 2^-32).
 //
 // The owner of a particle evaluates cos and sin of its phase once per step and
@@ -109,8 +112,8 @@ struct FastBuffers
   uint4 *aux0, *aux1;
   float2 *vel, *vel_tmp;
   unsigned *pid, *pid_tmp, *inv;
-  int2 *img, *img_tmp;
-  int *turns, *turns_tmp;
+  int2 *img;   // box crossings, by original index
+  int *turns;  // 2 pi turns of the phase, by original index
   int *cell_of, *cell_sorted;
   const int *cell_off;
   const int *order;
@@ -174,8 +177,8 @@ struct FastPath
   DeviceArray<uint4> rec[2], aux[2];
   DeviceArray<float2> vel, vel_tmp;
   DeviceArray<unsigned> pid, pid_tmp, inv;
-  DeviceArray<int2> img, img_tmp;
-  DeviceArray<int> turns, turns_tmp, cell_of, cell_sorted, vl_cnt, tile_maxcnt;
+  DeviceArray<int2> img;
+  DeviceArray<int> turns, cell_of, cell_sorted, vl_cnt, tile_maxcnt;
   DeviceArray<short> vl;
   DeviceArray<unsigned char> tiles;
   DeviceArray<SysParams> sys;
@@ -482,8 +485,8 @@ __global__ void fast_upload_kernel(const double *__restrict__ x, int n, int s, i
   (par ? B.rec1 : B.rec0)[q] = make_uint4((uint32_t) (X >> 32), (uint32_t) (Y >> 32), __float_as_uint(cp),
                                           __float_as_uint(sp));
   (par ? B.aux1 : B.aux0)[q] = make_uint4((uint32_t) X, (uint32_t) Y, ph, __float_as_uint(w));
-  B.img[q] = im;
-  B.turns[q] = (int) ft;
+  B.img[p] = im;
+  B.turns[p] = (int) ft;
   if (model == 2) B.vel[q] = make_float2((float) st[2], (float) st[3]);
 }
 
@@ -501,12 +504,12 @@ __global__ void fast_download_kernel(double *__restrict__ x, int n, int s, int m
     const unsigned q = B.inv[p];
     const uint4 r = (par ? B.rec1 : B.rec0)[q];
     const uint4 a = (par ? B.aux1 : B.aux0)[q];
-    const int2 im = B.img[q];
+    const int2 im = B.img[p];
     double *st = rows + s * threadIdx.x;
     st[0] = (double) im.x + (double) join64(r.x, a.x) * 5.421010862427522e-20;
     st[1] = (double) im.y + (double) join64(r.y, a.y) * 5.421010862427522e-20;
     const int ip = model == 1 ? 2 : 4;
-    st[ip] = 6.283185307179586 * ((double) B.turns[q] + (double) a.z * 2.3283064365386963e-10);
+    st[ip] = 6.283185307179586 * ((double) B.turns[p] + (double) a.z * 2.3283064365386963e-10);
     st[ip + 1] = (double) __uint_as_float(a.w);
     if (model == 2)
     {
@@ -545,8 +548,6 @@ __global__ void fast_permute_kernel(FastParams P, FastBuffers B)
   const unsigned p = B.pid[src];
   B.pid_tmp[q] = p;
   B.inv[p] = (unsigned) q;
-  B.img_tmp[q] = B.img[src];
-  B.turns_tmp[q] = B.turns[src];
   if (P.model == 2) B.vel_tmp[q] = B.vel[src];
   B.cell_sorted[q] = B.cell_of[src];
 }
@@ -556,8 +557,6 @@ __global__ void fast_copyback_kernel(FastParams P, FastBuffers B)
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= P.n) return;
   B.pid[q] = B.pid_tmp[q];
-  B.img[q] = B.img_tmp[q];
-  B.turns[q] = B.turns_tmp[q];
   if (P.model == 2) B.vel[q] = B.vel_tmp[q];
 }
 
@@ -1158,13 +1157,18 @@ __device__ __forceinline__ float advance_particle(const FastParams &P, const Fas
   phase_sincos(Pn, sn, cn);
   rout[q] = make_uint4((uint32_t) (Xn >> 32), (uint32_t) (Yn >> 32), __float_as_uint(cn), __float_as_uint(sn));
   aout[q] = make_uint4((uint32_t) Xn, (uint32_t) Yn, Pn, __float_as_uint(__fadd_rn(wi, dw)));
-  // box crossings and phase turns are rare: read-modify-write only then
-  if (cx | cy)
+  // box crossings and phase turns are rare: read-modify-write only then (the
+  // counts are kept by original index, so the slot re-sort never moves them)
+  if (cx | cy | ct)
   {
-    const int2 im = B.img[q];
-    B.img[q] = make_int2(im.x + cx, im.y + cy);
+    const unsigned p = B.pid[q];
+    if (cx | cy)
+    {
+      const int2 im = B.img[p];
+      B.img[p] = make_int2(im.x + cx, im.y + cy);
+    }
+    if (ct) B.turns[p] += ct;
   }
-  if (ct) B.turns[q] += ct;
   return fmaf(ddx, ddx, __fmul_rn(ddy, ddy));
 }
 
@@ -1946,9 +1950,7 @@ static FastBuffers buffers(spss_ctx *ctx)
   B.pid_tmp = f->pid_tmp.ptr;
   B.inv = f->inv.ptr;
   B.img = f->img.ptr;
-  B.img_tmp = f->img_tmp.ptr;
   B.turns = f->turns.ptr;
-  B.turns_tmp = f->turns_tmp.ptr;
   B.cell_of = f->cell_of.ptr;
   B.cell_sorted = f->cell_sorted.ptr;
   B.cell_off = f->binner.offsets.ptr;
@@ -2177,9 +2179,7 @@ int fast_create(spss_ctx *ctx)
   SPSS_TRY(f->pid_tmp.reserve(n));
   SPSS_TRY(f->inv.reserve(n));
   SPSS_TRY(f->img.reserve(n));
-  SPSS_TRY(f->img_tmp.reserve(n));
   SPSS_TRY(f->turns.reserve(n));
-  SPSS_TRY(f->turns_tmp.reserve(n));
   SPSS_TRY(f->cell_of.reserve(n));
   SPSS_TRY(f->cell_sorted.reserve(n));
   SPSS_TRY(f->vl_cnt.reserve(n));
@@ -2265,9 +2265,7 @@ void fast_destroy(spss_ctx *ctx)
   f->pid_tmp.release();
   f->inv.release();
   f->img.release();
-  f->img_tmp.release();
   f->turns.release();
-  f->turns_tmp.release();
   f->cell_of.release();
   f->cell_sorted.release();
   f->vl.release();
