@@ -1,4 +1,5 @@
 // Shared device utilities: prefix sum, stable cell binning, error recording.
+#include <climits>
 #include <cstdio>
 #include <cstring>
 
@@ -145,12 +146,38 @@ __global__ void bin_scatter_kernel(const int *__restrict__ cell_of, const int *_
   if (i < n) members[offsets[cell_of[i]] + slot[i]] = i;
 }
 
-// Members of one cell into ascending order (cells hold a handful of particles).
+// Members of one cell into ascending order (cells hold a handful of particles):
+// up to kSortRegs members are sorted in registers by an odd-even transposition
+// network (all loads issued together, one store each), larger cells by an
+// insertion sort in place.
+constexpr int kSortRegs = 8;
+
 __global__ void bin_sort_kernel(const int *__restrict__ offsets, int ncell, int *__restrict__ members)
 {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncell) return;
   const int b = offsets[c], e = offsets[c + 1];
+  const int m = e - b;
+  if (m <= 1) return;
+  if (m <= kSortRegs)
+  {
+    int v[kSortRegs];
+#pragma unroll
+    for (int k = 0; k < kSortRegs; ++k) v[k] = k < m ? members[b + k] : INT_MAX;
+#pragma unroll
+    for (int r = 0; r < kSortRegs; ++r)
+#pragma unroll
+      for (int k = r & 1; k + 1 < kSortRegs; k += 2)
+      {
+        const int lo = min(v[k], v[k + 1]), hi = max(v[k], v[k + 1]);
+        v[k] = lo;
+        v[k + 1] = hi;
+      }
+#pragma unroll
+    for (int k = 0; k < kSortRegs; ++k)
+      if (k < m) members[b + k] = v[k];
+    return;
+  }
   for (int q = b + 1; q < e; ++q)
   {
     const int v = members[q];
