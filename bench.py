@@ -13,8 +13,8 @@ field), mapped to the reference's unit box (L = sqrt(N / density)).
 Prints one JSON line.  `value`: particle-steps/s with the state resident in
 HBM (CUDA events on the library's stream, max over ranks, summed over ranks).
 `e2e`: the same through spss_step_host (host array in, host array out every
-step).  `roofline`: the pair-and-update kernel's algorithmic bytes over its
-CUDA-event duration.  `cpu_baseline` (rank 0): the oracle port of the
+step, the host array page-locked).  `roofline`: the pair-and-update kernel's
+algorithmic bytes over its CUDA-event duration.  `cpu_baseline` (rank 0): the oracle port of the
 reference algorithm on this host's cores.  `sweep`: 512 independent systems
 of the batched parameter sweep stepped as one batch (phase-diagram points
 per hour at 20,000 steps per point).  `surrogate` (rank 0): a 256 x 256
@@ -381,7 +381,7 @@ def run_legs_only(args, rank, world, local_rank):
 def run_ours(args, rank, world, local_rank):
     import torch
 
-    from spsslangevinintegration_gb300 import PRECISION_F32, Context, LINKED_LIST_VERLET
+    from spsslangevinintegration_gb300 import PRECISION_F32, Context, LINKED_LIST_VERLET, PinnedArray
     from spsslangevinintegration_gb300.replicas import max_over_ranks
 
     torch.cuda.set_device(local_rank)
@@ -435,10 +435,14 @@ def run_ours(args, rank, world, local_rank):
     achieved = bytes_per_launch / avg_kernel_s / 1e9
     traffic = traffic_per_launch()
 
-    # end to end through the host-array entry point (the drop-in DoStep path)
-    host = ctx.get_state()
+    # end to end through the host-array entry point (the drop-in DoStep path),
+    # the state in a page-locked host array the kernels read and write over
+    # the host link
+    pinned = PinnedArray(ctx.length)
+    host = pinned.array
+    host[:] = ctx.get_state()
     e2e_steps = max(1, min(args.steps, 10))
-    ctx.step_host(SRK, host, t, DT)  # registers the host array (pinned) once
+    ctx.step_host(SRK, host, t, DT)
     t += DT
     barrier()
     w0 = time.perf_counter()
@@ -448,6 +452,7 @@ def run_ours(args, rank, world, local_rank):
     barrier()
     e2e_s = max_over_ranks(time.perf_counter() - w0)
     e2e_value = world * n * e2e_steps / e2e_s
+    pinned.free()
     acc, flag, uses = ctx.verlet_state()
     ctx.close()
 
@@ -471,7 +476,8 @@ def run_ours(args, rank, world, local_rank):
                      "traffic": None if traffic is None else traffic * n},
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": n * 6 * 8,
                 "d2h_bytes_per_step": n * 6 * 8, "steps": e2e_steps,
-                "path": "spss_step_host: host AoS float64 in, one SRK step, host AoS out"},
+                "path": "spss_step_host: host AoS float64 in, one SRK step, host AoS out (page-locked host "
+                        "array from spss_pinned_alloc)"},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
         "verlet": {"accumulated_displacement": acc, "rebuild_pending": flag},

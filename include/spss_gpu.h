@@ -111,8 +111,12 @@ int spss_step(spss_ctx *ctx, int stepper, double t, double dt);
 /* nsteps consecutive DoStep calls, issued as one CUDA graph launch where possible. */
 int spss_steps(spss_ctx *ctx, int stepper, double t0, double dt, int nsteps);
 /* Drop-in DoStep(particle_system, system_state, t, dt) on a host AoS array:
- * copies it in, steps, copies it back (the host array is registered as
- * pinned memory on first use). */
+ * reads it in, steps, writes it back.  Pageable arrays are registered as
+ * mapped pinned memory on first use; page-locked mapped arrays
+ * (spss_pinned_alloc, cudaHostAlloc) are used as they are.  Either way the
+ * upload and download kernels read and write the array over the host link
+ * directly (StochasticRungeKuttaStepperPtr::DoStep, StochasticRungeKuttaStepperPtr.hpp:40-76,
+ * and the other steppers' DoStep). */
 int spss_step_host(spss_ctx *ctx, int stepper, double *state, long len, double t, double dt);
 int spss_get_step_counter(spss_ctx *ctx, unsigned long long *counter);
 int spss_set_step_counter(spss_ctx *ctx, unsigned long long counter);

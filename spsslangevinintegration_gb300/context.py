@@ -15,6 +15,33 @@ def make_params(model, n, rho, precision=N.PRECISION_F64, variant=N.VARIANT_DISP
                     rho, alpha, r_max, seed, replica)
 
 
+class PinnedArray:
+    """A page-locked, device-mapped host array (spss_pinned_alloc).  Passed to
+    Context.step_host, the upload and download kernels read and write it over
+    the host link directly (no registration, no staging copy); the observers'
+    frame buffers are of this kind too."""
+
+    def __init__(self, count, dtype=np.float64):
+        dtype = np.dtype(dtype)
+        ptr = ctypes.c_void_p()
+        N.check(N.lib().spss_pinned_alloc(int(count) * dtype.itemsize, ctypes.byref(ptr)), "spss_pinned_alloc")
+        self.ptr = ptr
+        raw = (ctypes.c_char * (int(count) * dtype.itemsize)).from_address(ptr.value)
+        self.array = np.frombuffer(raw, dtype=dtype, count=int(count))
+
+    def free(self):
+        if self.ptr:
+            self.array = None
+            N.lib().spss_pinned_free(self.ptr)
+            self.ptr = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.free()
+
+
 class Context:
     """One particle system on the GPU: state, interaction routine, steppers."""
 

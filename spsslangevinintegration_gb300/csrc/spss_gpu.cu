@@ -283,7 +283,7 @@ int spss_destroy(spss_ctx *ctx)
   ctx->frame_state.release();
   ctx->frame.release();
   ctx->average.release();
-  if (ctx->registered_host) cudaHostUnregister(ctx->registered_host);
+  if (ctx->registered_host && ctx->registered_here) cudaHostUnregister(ctx->registered_host);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -493,13 +493,23 @@ int spss_step_host(spss_ctx *ctx, int stepper, double *state, long len, double t
   const size_t bytes = sizeof(double) * len;
   if (ctx->registered_host != state || ctx->registered_bytes != bytes)
   {
-    if (ctx->registered_host) cudaHostUnregister(ctx->registered_host);
+    if (ctx->registered_host && ctx->registered_here) cudaHostUnregister(ctx->registered_host);
     ctx->registered_host = nullptr;
     ctx->registered_device = nullptr;
-    if (cudaHostRegister(state, bytes, cudaHostRegisterMapped) == cudaSuccess)
+    ctx->registered_here = false;
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, state) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
+        attr.devicePointer)
+    {
+      // already page-locked and mapped (spss_pinned_alloc, cudaHostAlloc): used as it is
+      ctx->registered_host = state;
+      ctx->registered_bytes = bytes;
+      ctx->registered_device = (double *) attr.devicePointer;
+    } else if (cudaHostRegister(state, bytes, cudaHostRegisterMapped) == cudaSuccess)
     {
       ctx->registered_host = state;
       ctx->registered_bytes = bytes;
+      ctx->registered_here = true;
       void *dp = nullptr;
       if (cudaHostGetDevicePointer(&dp, state, 0) == cudaSuccess) ctx->registered_device = (double *) dp;
       cudaGetLastError();

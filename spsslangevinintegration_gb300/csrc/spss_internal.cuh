@@ -292,6 +292,7 @@ struct spss_ctx
   void *registered_host = nullptr;
   size_t registered_bytes = 0;
   double *registered_device = nullptr;  // device view of the registered array (mapped pinned memory)
+  bool registered_here = false;         // registered by this context (else the caller's page-locked memory)
   spss::F64Path *f64 = nullptr;
   spss::FastPath *fast = nullptr;
   // AveragingObserver accumulator (FP64, AoS) and its count

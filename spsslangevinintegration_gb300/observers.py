@@ -13,13 +13,13 @@
   (SimulationEngineFirstOrder::InitializeSystemStateFromPreviousSolution,
   SimulationEngineFirstOrder.cpp:69-93).
 """
-import ctypes
 import os
 from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
 from . import _native as N
+from .context import PinnedArray
 
 
 def frame(ctx, wrapped=True):
@@ -29,22 +29,6 @@ def frame(ctx, wrapped=True):
     N.check(ctx.L.spss_frame_async(ctx.h, mode, N.fptr(out), out.size), "spss_frame_async")
     ctx.synchronize()
     return out
-
-
-class _Pinned:
-    """A page-locked float32 buffer."""
-
-    def __init__(self, count):
-        p = ctypes.c_void_p()
-        N.check(N.lib().spss_pinned_alloc(count * 4, ctypes.byref(p)), "spss_pinned_alloc")
-        self.ptr = p
-        self.array = np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_float)), shape=(count,))
-
-    def free(self):
-        if self.ptr:
-            N.lib().spss_pinned_free(self.ptr)
-            self.ptr = None
-            self.array = None
 
 
 class TrajectoryWriter:
@@ -60,7 +44,7 @@ class TrajectoryWriter:
         self.mode = N.FRAME_WRAPPED if (wrapped if wrapped is not None else ctx.model == 1) else N.FRAME_RAW
         self.traj = open(trajectory_path, "wb")
         self.summ = open(summary_path, "w") if summary_path else None
-        self.bufs = [_Pinned(ctx.length), _Pinned(ctx.length)]
+        self.bufs = [PinnedArray(ctx.length, np.float32), PinnedArray(ctx.length, np.float32)]
         self.pending = [None, None]
         self.pool = ThreadPoolExecutor(max_workers=1)
         self.counter = 0

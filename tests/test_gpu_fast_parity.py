@@ -134,6 +134,24 @@ def test_step_host_matches_device_steps():
         np.testing.assert_array_equal(a.get_state(), host)
 
 
+def test_step_host_on_pinned_array_equals_pageable():
+    """spss_step_host on a page-locked mapped array (PinnedArray, used in
+    place) and on a pageable array (registered by the library) give the same
+    bits."""
+    from spsslangevinintegration_gb300 import PinnedArray
+
+    p = params(2, 5000)
+    x0 = initial(2, 5000, 3, v=p["v0"])
+    with gpu_context(p, precision=F32, variant=2, seed=8) as a, gpu_context(p, precision=F32, variant=2, seed=8) as b:
+        host = x0.copy()
+        with PinnedArray(x0.size) as pin:
+            pin.array[:] = x0
+            for k in range(4):
+                a.step_host(1, host, (k + 1) * 0.005, 0.005)
+                b.step_host(1, pin.array, (k + 1) * 0.005, 0.005)
+            np.testing.assert_array_equal(pin.array, host)
+
+
 def test_upload_download_round_trip():
     p = params(2, 3000)
     x0 = initial(2, 3000, 4, v=p["v0"])
