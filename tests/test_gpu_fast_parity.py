@@ -179,6 +179,76 @@ def test_deterministic_and_noise_reproducible():
     np.testing.assert_array_equal(outs[0], outs[1])
 
 
+def band_pairs(model, seed):
+    """Isolated pairs at separations rho + m 2^-36 (rho = 2^-6 of the box,
+    m = -3..3), along x and along y, inside the box and across its periodic
+    edge; every coordinate a multiple of 2^-40, so the separations are exact
+    in FP64 and in the 64-bit fixed point alike.  Returns rho, the AoS state
+    and, per particle, whether its pair is within rho (m <= 0)."""
+    rho = 2.0 ** -6
+    pts, inside = [], []
+    for k, m in enumerate(range(-3, 4)):
+        d = rho + m * 2.0 ** -36
+        y = 0.0625 + 0.125 * k
+        pts += [(0.25, y), (0.25 + d, y)]                  # along x, inside
+        pts += [(1.0 - 2.0 ** -8, y), (d - 2.0 ** -8, y)]  # along x, across the edge
+        pts += [(0.5, y), (0.5, y + d)]                    # along y, inside
+        x = 0.5625 + 0.0625 * k
+        pts += [(x, 1.0 - 2.0 ** -8), (x, d - 2.0 ** -8)]  # along y, across the edge
+        inside += [m <= 0] * 8
+    pts = np.array(pts)
+    n = len(pts)
+    rng = np.random.default_rng(seed)
+    s = 4 if model == 1 else 6
+    x = np.zeros((n, s))
+    x[:, :2] = pts
+    phi = rng.uniform(-np.pi, np.pi, n)
+    if model == 1:
+        x[:, 2], x[:, 3] = phi, rng.uniform(-0.5, 0.5, n)
+    else:
+        x[:, 2], x[:, 3] = 1e-3 * np.cos(phi), 1e-3 * np.sin(phi)
+        x[:, 4], x[:, 5] = phi, rng.uniform(-0.5, 0.5, n)
+    return rho, x.reshape(-1), np.array(inside)
+
+
+@pytest.mark.parametrize("model,variant,stepper", [(1, 2, 2), (1, 4, 2), (1, 1, 1), (2, 2, 1), (2, 4, 2)])
+def test_cutoff_decisions_in_the_guard_band_match_fp64(model, variant, stepper):
+    """Every pair of band_pairs falls inside the FP32 guard band around
+    r = rho, so the FP64 decision from the 64-bit positions says whether it
+    interacts (m <= 0: in, m > 0: out).  One step equals the FP64 oracle's on
+    identical noise (one-step tolerance), and, particle by particle, equals
+    the oracle run with every pair in (rho + 2^-30) where m <= 0 and with
+    every pair out (rho - 2^-30) where m > 0, while differing from the other:
+    a wrong decision changes a neighbour count between 0 and 1."""
+    rho, x0, inside = band_pairs(model, 17)
+    n = inside.size
+    p = dict(model=model, n=n, rho=rho, flavor="ptr", v0=1e-3, sigma=1.0, alpha=0.2)
+    if model == 1:
+        p.update(xi=0.1, D_phi=0.1)
+    else:
+        p.update(xi_r=1.0, xi_phi=1.0, D_phi=0.1)
+    r_max = 1.3 * rho
+    kw = dict(r_max=r_max, nc_verlet=int(1.0 / r_max)) if variant == 4 else {}
+    s = 4 if model == 1 else 6
+    with gpu_context(p, precision=F32, variant=variant, seed=23, **kw) as ctx:
+        ctx.set_state(x0)
+        normals = ctx.noise(stepper, 0)
+        ctx.step(stepper, 0.005, 0.005)
+        got = ctx.get_state()
+
+    def oracle_step(rho_o):
+        x = x0.copy()
+        oracle_system(dict(p, rho=rho_o), **kw).step(stepper, variant, x, 0.005, 0.005, normals)
+        return x
+
+    ref, all_in, all_out = oracle_step(rho), oracle_step(rho + 2.0 ** -30), oracle_step(rho - 2.0 ** -30)
+    assert state_err(got, ref, s).max() <= 1e-5
+    e_in = state_err(got, all_in, s).max(axis=1)
+    e_out = state_err(got, all_out, s).max(axis=1)
+    assert np.all(e_in[inside] <= 1e-5) and np.all(e_out[~inside] <= 1e-5)
+    assert np.all(e_out[inside] > 5e-5) and np.all(e_in[~inside] > 5e-5)
+
+
 @pytest.mark.parametrize("model,stepper,per", [(2, 2, 6), (2, 1, 3), (1, 2, 2), (1, 1, 1)])
 def test_fast_noise_is_standard_normal_and_independent(model, stepper, per):
     """The fast path's normals (six from one Philox block for second-order SRK,
