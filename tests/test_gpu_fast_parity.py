@@ -179,6 +179,31 @@ def test_deterministic_and_noise_reproducible():
     np.testing.assert_array_equal(outs[0], outs[1])
 
 
+@pytest.mark.parametrize("model,variant,stepper,n,density", [
+    (2, 2, 1, 1, 2.0), (2, 2, 1, 2, 2.0), (2, 4, 2, 7, 2.0), (1, 2, 2, 5, 0.5), (1, 4, 1, 40, 2.0),
+    (2, 2, 2, 64, 8.0), (1, 4, 2, 64, 2.0)])
+def test_tiny_systems_match_fp64_oracle(model, variant, stepper, n, density):
+    """Systems of 1 to 64 particles: one to six cells per side, so stencils
+    wrap onto the same cells several times (as the reference's do) and Verlet
+    lists can exceed their capacity (the step then scans the stencil)."""
+    p = params(model, n, density=density)
+    x0 = initial(model, n, 31 + n, v=p["v0"])
+    r_max = 1.3 * p["rho"]
+    nc_v = max(1, int(1.0 / r_max))
+    s = 4 if model == 1 else 6
+    with gpu_context(p, precision=F32, variant=variant, r_max=r_max, nc_verlet=nc_v, seed=29) as ctx:
+        orc = oracle_system(p, r_max=r_max, nc_verlet=nc_v)
+        ctx.set_state(x0)
+        x = x0.copy()
+        for k in range(3):
+            normals = ctx.noise(stepper, k)
+            ctx.step(stepper, (k + 1) * 0.005, 0.005)
+            orc.step(stepper, variant, x, (k + 1) * 0.005, 0.005, normals)
+        got = ctx.get_state()
+    assert np.all(np.isfinite(got))
+    assert state_err(got, x, s).max() <= 1e-5
+
+
 def band_pairs(model, seed):
     """Isolated pairs at separations rho + m 2^-36 (rho = 2^-6 of the box,
     m = -3..3), along x and along y, inside the box and across its periodic
