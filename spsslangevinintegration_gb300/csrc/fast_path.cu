@@ -983,12 +983,39 @@ __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const Fa
     int m = 0;
     for (; m + 4 <= cnt; m += 4)
     {
-      const int i0 = lp[0], i1 = lp[n], i2 = lp[2 * n], i3 = lp[3 * n];
+      // four candidates as one group: entries, records and omega words loaded
+      // together, four FP32 distances, one guard-band test for the group (a
+      // group with a candidate inside the band is redone one by one with the
+      // FP64 decision there), so the common path has no branch between loads
+      const int i[4] = {lp[0], lp[n], lp[2 * n], lp[3 * n]};
       lp += 4 * n;
-      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, L, aux, i0, a);
-      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, L, aux, i1, a);
-      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, L, aux, i2, a);
-      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, L, aux, i3, a);
+      uint4 r[4];
+      float w[4], d2[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+      {
+        r[k] = srec[i[k]];
+        w[k] = OMEGA ? __uint_as_float(saux[i[k]].w) : 0.0f;
+      }
+      bool band = false;
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+      {
+        const float dx = (float) (int) (r[k].x - ri.x);
+        const float dy = (float) (int) (r[k].y - ri.y);
+        d2[k] = fmaf(dx, dx, dy * dy);
+        band |= fabsf(d2[k] - P.rho2_f) <= P.band_f;
+      }
+      if (!band)
+      {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (d2[k] <= P.rho2_f) accumulate(a, r[k], w[k]);
+      } else
+      {
+#pragma unroll 1
+        for (int k = 0; k < 4; ++k) candidate_staged<OMEGA, true>(P, ri, Xi, Yi, srec, saux, L, aux, i[k], a);
+      }
     }
     for (; m < cnt; ++m)
     {
