@@ -30,10 +30,16 @@ class PinnedArray:
         self.array = np.frombuffer(raw, dtype=dtype, count=int(count))
 
     def free(self):
-        if self.ptr:
+        if getattr(self, "ptr", None):
             self.array = None
             N.lib().spss_pinned_free(self.ptr)
             self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
     def __enter__(self):
         return self
