@@ -404,7 +404,10 @@ def run_ours(args, rank, world, local_rank):
             dist.barrier()
         torch.cuda.synchronize()
 
-    # warm-up (includes graph capture and the first list build)
+    # tile width and launch form picked by the library's autotuner (trial
+    # steps, state restored), then warm-up (graph capture, first list build)
+    tune_ms = None if args.no_autotune else ctx.autotune(SRK, DT, steps=4)
+    tiling = ctx.tiling()
     t = 0.0
     ctx.steps(SRK, t, DT, args.warmup)
     t += DT * args.warmup
@@ -468,7 +471,8 @@ def run_ours(args, rank, world, local_rank):
                                "v0=0.5, sigma=1, D=0.1; one independent replica per GPU" % n,
                    "n": n, "l2": "inputs larger than L2 (state %.0f MB + lists %.0f MB)" % (
                        n * 56 / 1e6, n * 4 * (mean_list_length(p) + 1) / 1e6),
-                   "parallelism": "replicas x%d" % world},
+                   "parallelism": "replicas x%d" % world,
+                   "tiling": {"tile_cells": tiling[0], "persistent": tiling[1], "autotuned_ms_per_step": tune_ms}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "kernel": "fast_tile_kernel<2,2,2> (pair sums + SRK update)",
                      "kernel_ms": avg_kernel_s * 1e3,
@@ -503,6 +507,8 @@ def main():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="main leg: keep the default tiling (32 cells per tile, one launch per step)")
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--sweep-steps", type=int, default=400)
     ap.add_argument("--no-surrogate", action="store_true")
