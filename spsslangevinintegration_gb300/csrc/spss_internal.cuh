@@ -164,16 +164,6 @@ __device__ __forceinline__ void box_muller6_f32(const uint4 &u, float z[6])
   }
 }
 
-// Normal number d (0-based, reference draw order) of one particle at one step.
-__device__ __forceinline__ double normal_f64(const NoiseKey &nk, uint32_t particle, int d)
-{
-  const uint4 u = philox_block(nk, particle, (uint32_t) (d >> 2));
-  double z0, z1;
-  if ((d & 3) < 2) box_muller_f64(u.x, u.y, z0, z1);
-  else box_muller_f64(u.z, u.w, z0, z1);
-  return (d & 1) ? z1 : z0;
-}
-
 __device__ __forceinline__ void normals4_f32(const NoiseKey &nk, uint32_t particle, uint32_t block, float z[4])
 {
   const uint4 u = philox_block(nk, particle, block);
