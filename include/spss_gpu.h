@@ -248,7 +248,7 @@ int spss_batch_reset_stats(spss_ctx *ctx);
  * on the tiling; the lists are rebuilt before the next step.  F32 contexts. */
 int spss_set_tiling(spss_ctx *ctx, int tile_cells, int persistent);
 int spss_get_tiling(spss_ctx *ctx, int *tile_cells, int *persistent);
-/* Times `steps` steps of every tiling candidate (16 to 64 cells per tile in steps of 8,
+/* Times `steps` steps of every tiling candidate (16 to 64 cells per tile in steps of 4,
  * both launch forms) on the context's current state, keeps the fastest and
  * restores the state, step counter and trigger as they were (the lists are
  * rebuilt before the next step; before the first step that leaves every

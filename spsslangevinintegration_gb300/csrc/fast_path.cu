@@ -2782,7 +2782,7 @@ int fast_autotune(spss_ctx *ctx, int stepper, double dt, int steps, double *best
   const int timing = ctx->timing;
   ctx->timing = 0;
   SPSS_TRY(take_snapshot(ctx));
-  const int widths[] = {16, 24, 32, 40, 48, 56, 64};
+  const int widths[] = {16, 20, 24, 28, 32, 36, 40, 44, 48, 52, 56, 60, 64};
   double best = 1e300;
   int best_w = f->tile_cells, best_p = f->persistent;
   int rc = SPSS_OK;
