@@ -104,7 +104,7 @@ def test_graph_steps_equal_single_steps_bitwise():
 
 
 def test_verlet_equals_linked_list_at_benchmark_size():
-    """Config-3 size: the Verlet path (skin 0.3 R, rebuilt on the displacement
+    """Benchmark size (N = 4,194,304): the Verlet path (skin 0.3 R, rebuilt on the displacement
     trigger) and the per-step cell list see the same neighbour sets, so the
     trajectories agree to FP32 summation-order differences."""
     n = 4194304
