@@ -64,7 +64,7 @@ case("fo_rhs_allpairs_serial", model=1, flavor="serial", mode="rhs", variant=1, 
      dt=0.01, seed=1, **P1)
 case("fo_rhs_allpairs_ptr", model=1, flavor="ptr", mode="rhs", variant=1, n=200, rho=0.12, k_coef=0.5, dt=0.01,
      seed=2, higher_order=1, outside=6, **P1)
-case("fo_rhs_allpairs_config1", model=1, flavor="serial", mode="rhs", variant=1, n=1000, rho=1 / np.sqrt(1000.0),
+case("fo_rhs_allpairs_n1000", model=1, flavor="serial", mode="rhs", variant=1, n=1000, rho=1 / np.sqrt(1000.0),
      k_coef=0.0, dt=0.01, seed=3, v0=0.1 / np.sqrt(1000.0), xi=0.1, sigma=1.0, alpha=0.0, D_phi=0.0)
 case("fo_rhs_linkedlist_serial", model=1, flavor="serial", mode="rhs", variant=2, n=400, rho=0.08, k_coef=0.5,
      dt=0.01, seed=4, outside=8, **P1)
@@ -91,7 +91,7 @@ case("fo_rk4_verlet_serial", model=1, flavor="serial", mode="step", stepper="rk4
      nsteps=10, seed=13, **P1s)
 case("fo_rk4_allpairs_serial", model=1, flavor="serial", mode="step", stepper="rk4", n=150, rho=0.6, dt=0.01,
      nsteps=5, seed=14, **P1s)
-case("fo_rk4direct_allpairs_config1", model=1, flavor="serial", mode="step", stepper="rk4_direct", variant=1,
+case("fo_rk4direct_allpairs_n1000", model=1, flavor="serial", mode="step", stepper="rk4_direct", variant=1,
      n=1000, rho=1 / np.sqrt(1000.0), dt=0.01, nsteps=3, seed=15, v0=0.1 / np.sqrt(1000.0), xi=0.1, sigma=1.0,
      alpha=0.0, D_phi=0.0)
 case("fo_se_llverlet_ptr", model=1, flavor="ptr", mode="step", stepper="se", n=400, rho=0.1, dt=0.01, nsteps=25,
