@@ -15,7 +15,9 @@ HBM (CUDA events on the library's stream, max over ranks, summed over ranks).
 `e2e`: the same through spss_step_host (host array in, host array out every
 step, the host array page-locked).  `roofline`: the pair-and-update kernel's
 algorithmic bytes over its CUDA-event duration.  `cpu_baseline` (rank 0): the oracle port of the
-reference algorithm on this host's cores.  `sweep`: 512 independent systems
+reference algorithm on this host's cores.  `cells`: the same workload with
+cell lists rebuilt every step (the reference's linked list) next to the
+oracle port of that cell-list workload.  `sweep`: 512 independent systems
 of the batched parameter sweep stepped as one batch (phase-diagram points
 per hour at 20,000 steps per point).  `surrogate` (rank 0): a 256 x 256
 phase diagram from the learned surrogate with an active-learning round,
@@ -184,6 +186,76 @@ def cpu_baseline(n, budget_s=20.0, bench_lib=True):
     return {"value": n * steps / el, "unit": "particle-steps/s", "cores": cores, "kind": "port",
             "sample": "N=%d second-order SRK, linked-list+Verlet skin 0.3R, %d timed steps after 1 warm-up "
                       "step (%.1f s), FP64 oracle port, OpenMP %d threads" % (n, steps, el, cores)}
+
+
+def cpu_cells_sample(n, budget_s=8.0):
+    """The oracle port on this host's cores on the cell-list form of the
+    workload (linked list rebuilt at every evaluation, as the reference's),
+    for a bounded number of steps."""
+    from oracle import binding as ob
+
+    cores = os.cpu_count() or 1
+    ob.set_threads(cores, bench=True)
+    p, L = workload(n)
+    sysm = ob.System(2, n, p["rho"], v0=p["v0"], xi_r=p["xi_r"], D_r=p["D_r"], xi_phi=p["xi_phi"],
+                     D_phi=p["D_phi"], sigma=p["sigma"], alpha=p["alpha"], bench=True)
+    x = initial_state(n, L, 0)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        normals = ob.philox_normals(0, steps, 0, 6 * n, bench=True)
+        sysm.step(ob.SRK, 2, x, DT * (steps + 1), DT, normals)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or steps >= 50:
+            break
+    sysm.close()
+    return {"value": n * steps / el, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+            "sample": "N=%d second-order SRK, linked list rebuilt every step, %d timed steps (%.1f s), FP64 "
+                      "oracle port, OpenMP %d threads" % (n, steps, el, cores)}
+
+
+def run_cells_leg(args, rank, world, barrier, max_over_ranks):
+    """The main leg's workload with cell lists rebuilt every step (the
+    reference's linked list) instead of Verlet lists, device-timed, next to
+    the oracle port of the same cell-list workload on the host cores."""
+    import torch
+
+    from spsslangevinintegration_gb300 import PRECISION_F32, Context, LINKED_LIST
+
+    n = args.n
+    p, L = workload(n)
+    ctx = Context(2, n, p["rho"], precision=PRECISION_F32, variant=LINKED_LIST, v0=p["v0"], xi_r=p["xi_r"],
+                  D_r=p["D_r"], xi_phi=p["xi_phi"], D_phi=p["D_phi"], sigma=p["sigma"], alpha=p["alpha"],
+                  seed=12345, replica=rank)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_state(initial_state(n, L, rank))
+    tune_ms = ctx.autotune(SRK, DT, steps=4)
+    tiling = ctx.tiling()
+    ctx.steps(SRK, 0.0, DT, max(3, args.warmup // 4))
+    steps = max(20, min(args.steps, 100))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(stream)
+    ctx.steps(SRK, 0.0, DT, steps)
+    e1.record(stream)
+    barrier()
+    ms = max_over_ranks(e0.elapsed_time(e1))
+    ctx.close()
+    if rank != 0:
+        return None
+    value = world * n * steps / (ms * 1e-3)
+    out = {"workload": "the main workload (N=%d, SRK) with cell lists of side 1/int(1/rho) rebuilt every step "
+                       "(slot re-sort and tile layout each step)" % n,
+           "value": value, "unit": "particle-steps/s", "ms_per_step": ms / steps, "steps_timed": steps,
+           "tiling": {"tile_cells": tiling[0], "persistent": tiling[1], "autotuned_ms_per_step": tune_ms},
+           "timing": "CUDA events around %d graph steps on the library's stream, max over ranks" % steps}
+    if not args.no_cpu_baseline and world == 1:
+        cpu = cpu_cells_sample(n)
+        out["cpu_baseline"] = cpu
+        out["speedup_vs_cpu"] = value / cpu["value"]
+    return out
 
 
 SWEEP_SYSTEMS, SWEEP_STEPS_PER_POINT, SWEEP_SAMPLE_EVERY = 512, 20000, 10
@@ -367,6 +439,10 @@ def run_legs_only(args, rank, world, local_rank):
         torch.cuda.synchronize()
 
     line = {"legs": sorted(args.legs)}
+    if "cells" in args.legs:
+        cl = run_cells_leg(args, rank, world, barrier, max_over_ranks)
+        if cl is not None:
+            line["cells"] = cl
     if "sweep" in args.legs:
         sw = run_sweep_leg(args, rank, world, barrier, max_over_ranks)
         if sw is not None:
@@ -488,6 +564,10 @@ def run_ours(args, rank, world, local_rank):
     }
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(n, budget_s=args.cpu_seconds)
+    if not args.no_cells:
+        cl = run_cells_leg(args, rank, world, barrier, max_over_ranks)
+        if cl is not None:
+            line["cells"] = cl
     if not args.no_sweep:
         sw = run_sweep_leg(args, rank, world, barrier, max_over_ranks)
         if sw is not None:
@@ -513,8 +593,8 @@ def main():
     ap.add_argument("--sweep-steps", type=int, default=400)
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--surrogate-train", type=int, default=50000)
-    ap.add_argument("--legs", default="main,sweep,surrogate",
-                    help="comma-separated subset of main, sweep, surrogate (profiling a leg alone)")
+    ap.add_argument("--legs", default="main,cells,sweep,surrogate",
+                    help="comma-separated subset of main, cells, sweep, surrogate (profiling a leg alone)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -528,6 +608,7 @@ def main():
 
         dist.init_process_group("nccl")
     args.legs = set(x.strip() for x in args.legs.split(",") if x.strip())
+    args.no_cells = "cells" not in args.legs
     if "main" in args.legs:
         args.no_sweep = args.no_sweep or "sweep" not in args.legs
         args.no_surrogate = args.no_surrogate or "surrogate" not in args.legs
