@@ -88,3 +88,18 @@ def test_cpp_dropin_example_compiles_and_links(tmp_path):
                     os.path.join(ROOT, "tests", "cpp", "dropin_example.cpp"), "-o", exe, "-pthread",
                     "-L" + os.path.dirname(lib), "-lspss_gpu", "-Wl,-rpath," + os.path.dirname(lib)], check=True)
     assert os.path.getsize(exe) > 0
+
+
+def test_no_cpu_fallback_without_a_gpu():
+    """Without a GPU the library refuses to create a context (a CUDA error
+    code, raised as SpssError) instead of computing on the CPU."""
+    import pytest
+
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from spsslangevinintegration_gb300 import LINKED_LIST, PRECISION_F32, Context, SpssError
+
+    built_library()
+    with pytest.raises(SpssError):
+        Context(2, 1000, 0.05, precision=PRECISION_F32, variant=LINKED_LIST)
