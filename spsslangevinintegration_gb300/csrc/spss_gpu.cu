@@ -626,7 +626,7 @@ int spss_average_get(spss_ctx *ctx, double *mean_state, long len, int *count)
   SPSS_CUDA_TRY(cudaMemcpyAsync(mean_state, ctx->average.ptr, sizeof(double) * len, cudaMemcpyDeviceToHost,
                                 ctx->stream));
   SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-  // AveragingObserver.cpp:294: accumulated / number_of_accumulated_steps
+  // AveragingObserver.cpp:62-64: accumulated / number_of_accumulated_steps
   for (long q = 0; q < len; ++q) mean_state[q] /= ctx->average_count;
   return SPSS_OK;
 }

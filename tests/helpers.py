@@ -109,3 +109,44 @@ def reference_frame(x, s, wrapped):
         out[:, ip] = (d - np.floor(d / two_pi) * two_pi).astype(np.float32)
         f = out
     return f.reshape(-1)
+
+
+def config_system(model, n, density, R=1.0, v0=0.5, m=1.0, D=0.1, sigma=1.0, alpha=0.0, xi=0.1):
+    """The benchmark configurations' physical parameters in the reference's
+    unit box: L = sqrt(N / density), rho = R / L, v0 -> v0 / L; second order
+    xi_r = xi_phi = 1 / m, sigma -> sigma / m, D_phi = D / m^2, D_r = 0;
+    first order the reference's default friction xi = 0.1 and D_phi = D."""
+    L = np.sqrt(n / density)
+    p = dict(model=model, n=n, rho=R / L, flavor="ptr", v0=v0 / L, alpha=alpha)
+    if model == 1:
+        p.update(xi=xi, sigma=sigma, D_phi=D)
+    else:
+        p.update(xi_r=1.0 / m, xi_phi=1.0 / m, D_r=0.0, D_phi=D / m ** 2, sigma=sigma / m)
+    return p, L
+
+
+def config_initial(model, n, L, seed):
+    """Uniform positions in the unit box, phases uniform in [-pi, pi),
+    omega = 0; second order: velocity the unit vector along phi divided by L
+    (SimulationEngineSecondOrder.cpp:46-50)."""
+    rng = np.random.default_rng(seed)
+    s = 4 if model == 1 else 6
+    x = np.zeros((n, s))
+    x[:, 0], x[:, 1] = rng.random(n), rng.random(n)
+    phi = rng.uniform(-np.pi, np.pi, n)
+    if model == 1:
+        x[:, 2] = phi
+    else:
+        x[:, 2], x[:, 3], x[:, 4] = np.cos(phi) / L, np.sin(phi) / L, phi
+    return x.reshape(-1)
+
+
+def state_err(got, ref, s):
+    """Per-component error |got - ref| / (|ref| + max |ref| of the component),
+    positions under the minimum image with unit scale."""
+    got, ref = np.asarray(got).reshape(-1, s), np.asarray(ref).reshape(-1, s)
+    d = got - ref
+    d[:, :2] = min_image(d[:, :2])
+    scale = np.abs(ref).max(axis=0)
+    scale[:2] = 1.0
+    return np.abs(d) / (np.abs(ref) + scale)
