@@ -15,16 +15,36 @@
 //   StochasticRungeKuttaStepperPtr  Steppers/StochasticRungeKuttaStepperPtr.hpp:21-85
 //   PeriodicBoundaryConditions      BoundaryConfiguration/PeriodicBoundaryConditions.hpp:12-48
 //   Thread, ThreadSharedMemory      Parallelization/Thread.hpp:12-41, ThreadSharedMemory.hpp:15-53
-//   AveragingObserver               Observers/AveragingObserver.hpp:12-35
-//   BinaryObserver{First,Second}Order (SaveSummaryStatistics, SaveSystemState)
+//   AveragingObserver[Ptr]          Observers/AveragingObserver.hpp:12-35, AveragingObserverPtr.hpp:14-37
+//   BinaryObserverFirstOrder[Ptr]   Observers/BinaryObserverFirstOrder.hpp:18-50, BinaryObserverFirstOrderPtr.hpp:18-51
+//   BinaryObserverSecondOrder[Ptr]  Observers/BinaryObserverSecondOrder.hpp:16-55, BinaryObserverSecondOrderPtr.hpp:16-57
+//
+// State residency.  DoStep runs on the GPU and writes the stepped state back
+// into the caller's host array; the GPU keeps a copy.  The library remembers,
+// per particle system, which host array that copy mirrors (the array most
+// recently passed to its DoStep).  PeriodicBoundaryConditions wraps such an
+// array on the host as the reference does and wraps the GPU copy with it, and
+// the observers read the GPU copy of such an array (GPU order-parameter
+// reduction, frames converted on the GPU) instead of looping over the host
+// array.  A program that changes a stepped array on the host by other means
+// before an observer reads it calls spss::HostStateChanged(array) first; the
+// observers then read the host array.
 #ifndef SPSS_DROPIN_HPP
 #define SPSS_DROPIN_HPP
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <functional>
+#include <iomanip>
+#include <iostream>
+#include <mutex>
 #include <numeric>
+#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <thread>
@@ -69,6 +89,126 @@ inline unsigned long long &default_seed()
   static unsigned long long s = 0;
   return s;
 }
+
+// Folder the reference-named observers write into (the reference compiles a
+// machine-specific folder into each observer).  Default: the environment
+// variable SPSS_OUTPUT_FOLDER, else the working directory; include the
+// trailing '/'.
+inline std::string &output_folder()
+{
+  static std::string folder = [] {
+    const char *env = std::getenv("SPSS_OUTPUT_FOLDER");
+    return std::string(env ? env : "");
+  }();
+  return folder;
+}
+
+// The observers print the reference's "value at t = ... integrated in ...s"
+// line on every saved frame; false silences it.
+inline bool &observer_progress_lines()
+{
+  static bool on = true;
+  return on;
+}
+
+namespace detail
+{
+
+// Host arrays mirrored on the GPU: array -> context whose device state is a
+// copy of it (set by DoStep; a context mirrors one array at a time).
+struct Resident
+{
+  const void *host;
+  spss_ctx *ctx;
+};
+
+inline std::mutex &resident_mutex()
+{
+  static std::mutex m;
+  return m;
+}
+
+inline std::vector<Resident> &residents()
+{
+  static std::vector<Resident> r;
+  return r;
+}
+
+inline void set_resident(const void *host, spss_ctx *ctx)
+{
+  std::lock_guard<std::mutex> lock(resident_mutex());
+  auto &r = residents();
+  r.erase(std::remove_if(r.begin(), r.end(), [&](const Resident &e) { return e.host == host || e.ctx == ctx; }),
+          r.end());
+  r.push_back({host, ctx});
+}
+
+inline void drop_resident_host(const void *host)
+{
+  std::lock_guard<std::mutex> lock(resident_mutex());
+  auto &r = residents();
+  r.erase(std::remove_if(r.begin(), r.end(), [&](const Resident &e) { return e.host == host; }), r.end());
+}
+
+inline void drop_resident_ctx(spss_ctx *ctx)
+{
+  std::lock_guard<std::mutex> lock(resident_mutex());
+  auto &r = residents();
+  r.erase(std::remove_if(r.begin(), r.end(), [&](const Resident &e) { return e.ctx == ctx; }), r.end());
+}
+
+inline spss_ctx *resident(const void *host)
+{
+  std::lock_guard<std::mutex> lock(resident_mutex());
+  for (const Resident &e : residents())
+    if (e.host == host) return e.ctx;
+  return nullptr;
+}
+
+// Called with a context just before a drop-in particle system destroys it.
+struct ContextListener
+{
+  int id;
+  std::function<void(spss_ctx *)> fn;
+};
+
+inline std::vector<ContextListener> &context_listeners()
+{
+  static std::vector<ContextListener> l;
+  return l;
+}
+
+inline int add_context_listener(std::function<void(spss_ctx *)> fn)
+{
+  std::lock_guard<std::mutex> lock(resident_mutex());
+  static int next = 0;
+  context_listeners().push_back({++next, std::move(fn)});
+  return next;
+}
+
+inline void remove_context_listener(int id)
+{
+  std::lock_guard<std::mutex> lock(resident_mutex());
+  auto &l = context_listeners();
+  l.erase(std::remove_if(l.begin(), l.end(), [&](const ContextListener &e) { return e.id == id; }), l.end());
+}
+
+inline void notify_context_destroyed(spss_ctx *ctx)
+{
+  std::vector<ContextListener> copy;
+  {
+    std::lock_guard<std::mutex> lock(resident_mutex());
+    copy = context_listeners();
+  }
+  for (auto &e : copy) e.fn(ctx);
+}
+
+}  // namespace detail
+
+// The program changed `state` on the host after the last DoStep on it: the
+// GPU copy no longer mirrors it, and the observers read the host array until
+// the next DoStep.
+inline void HostStateChanged(const Real *state) { detail::drop_resident_host(state); }
 
 }  // namespace spss
 
@@ -140,6 +280,9 @@ class PeriodicBoundaryConditions
     x_pbc = x - std::floor(x * x_rsize_) * x_size_;
     y_pbc = y - std::floor(y * y_rsize_) * y_size_;
   }
+  // PeriodicBoundaryConditions::ApplyPeriodicBoundaryConditions (PeriodicBoundaryConditions.cpp:127-155):
+  // the host array as the reference wraps it and, when the array is mirrored
+  // on the GPU (the last array a drop-in DoStep stepped), the GPU copy too.
   template<class V>
   void ApplyPeriodicBoundaryConditions(V &system_state)
   {
@@ -148,6 +291,7 @@ class PeriodicBoundaryConditions
       system_state[s_ * i] -= std::floor(system_state[s_ * i] * x_rsize_) * x_size_;
       system_state[s_ * i + 1] -= std::floor(system_state[s_ * i + 1] * y_rsize_) * y_size_;
     }
+    WrapMirror(&system_state[0]);
   }
   void ApplyPeriodicBoundaryConditions(Real *const system_state, long)
   {
@@ -156,11 +300,17 @@ class PeriodicBoundaryConditions
       system_state[s_ * i] -= std::floor(system_state[s_ * i] * x_rsize_) * x_size_;
       system_state[s_ * i + 1] -= std::floor(system_state[s_ * i + 1] * y_rsize_) * y_size_;
     }
+    WrapMirror(system_state);
   }
   Real GetXSize() const { return x_size_; }
   Real GetYSize() const { return y_size_; }
 
  private:
+  void WrapMirror(const void *host)
+  {
+    if (spss_ctx *ctx = spss::detail::resident(host)) spss::check(spss_apply_pbc(ctx), "ApplyPeriodicBoundaryConditions");
+  }
+
   Thread *thread_;
   int n_, s_;
   Real x_size_, y_size_, x_rsize_, y_rsize_;
@@ -203,13 +353,21 @@ class SystemBase
   SystemBase &operator=(const SystemBase &) = delete;
   ~SystemBase()
   {
-    if (ctx_) spss_destroy(ctx_);
+    if (ctx_)
+    {
+      detail::notify_context_destroyed(ctx_);
+      detail::drop_resident_ctx(ctx_);
+      spss_destroy(ctx_);
+    }
   }
 
-  // Stepper entry: the context runs DoStep on the caller's host array.
+  // Stepper entry: the context runs DoStep on the caller's host array, whose
+  // copy then stays on the GPU for the observers.
   void Step(int stepper, Real *state, Real t, Real dt)
   {
+    detail::drop_resident_ctx(ctx_);
     check(spss_step_host(ctx_, stepper, state, (long) n_ * s_, t, dt), "DoStep");
+    detail::set_resident(state, ctx_);
     RefreshFlags();
   }
   spss_ctx *context() { return ctx_; }
@@ -223,6 +381,8 @@ class SystemBase
     p.nc_verlet = nc_verlet;
     spss_ctx *c = nullptr;
     check(spss_create(&p, &c), "spss_create");
+    detail::notify_context_destroyed(ctx_);
+    detail::drop_resident_ctx(ctx_);
     spss_destroy(ctx_);
     ctx_ = c;
     params_ = p;
@@ -531,169 +691,527 @@ class StochasticRungeKuttaStepperPtr
 
 // ------------------------------------------------------------------ observers
 
-// AveragingObserver (Observers/AveragingObserver.cpp:29-69): running sum of the state.
-class AveragingObserver
+namespace spss
+{
+namespace detail
+{
+
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+
+// The .bin trajectory file of a binary observer: frames [float t][float s*n]
+// (BinaryObserverFirstOrder.cpp:119-120).  Frames of a GPU-mirrored state are
+// converted on the GPU (spss_frame_async) into one of two page-locked
+// buffers and written by a background thread while the next steps run;
+// frames of a host array are converted and written on the calling thread.
+// Frames reach the file in call order.
+class FrameFile
 {
  public:
-  AveragingObserver(int number_of_particles, int number_of_state_variables)
-      : n_(number_of_particles), s_(number_of_state_variables), acc_((size_t) number_of_particles * number_of_state_variables, 0.0)
-  {}
-  void operator()(const std::vector<Real> &x, Real)
+  FrameFile(const std::string &path, long len) : len_(len)
   {
-    for (size_t q = 0; q < acc_.size(); ++q) acc_[q] += x[q];
-    ++count_;
+    std::remove(path.c_str());
+    file_ = std::fopen(path.c_str(), "ab");
+    if (!file_) throw Error(SPSS_ERR_INVALID_ARGUMENT, ("cannot open " + path).c_str());
   }
-  // averaged omega (index 3) as float, as SaveAveragedSystemState writes it (AveragingObserver.cpp:291-297)
-  std::vector<RealOutput> AveragedAngularVelocities() const
+  FrameFile(const FrameFile &) = delete;
+  FrameFile &operator=(const FrameFile &) = delete;
+  ~FrameFile()
   {
-    std::vector<RealOutput> out((size_t) n_);
-    for (int i = 0; i < n_; ++i) out[i] = acc_[(size_t) s_ * i + 3] / count_;
-    return out;
+    Flush();
+    for (float *b : buf_)
+      if (b) spss_pinned_free(b);
+    if (file_) std::fclose(file_);
   }
-  void SaveAveragedSystemState(const std::string &file_name) const
+  void Flush()
   {
-    std::vector<RealOutput> w = AveragedAngularVelocities();
-    FILE *f = std::fopen(file_name.c_str(), "wb");
-    if (!f) throw spss::Error(SPSS_ERR_INVALID_ARGUMENT, "SaveAveragedSystemState");
-    std::fwrite(w.data(), sizeof(RealOutput), w.size(), f);
-    std::fclose(f);
+    for (auto &w : writer_)
+      if (w.joinable()) w.join();
   }
-  int count() const { return count_; }
+  // The frame of the state `ctx` holds (SPSS_FRAME_RAW or SPSS_FRAME_WRAPPED).
+  void WriteDevice(spss_ctx *ctx, int mode, float t)
+  {
+    const int b = next_;
+    if (writer_[b].joinable()) writer_[b].join();  // this buffer's previous frame is on disk
+    if (!buf_[b]) check(spss_pinned_alloc(sizeof(float) * (size_t) len_, (void **) &buf_[b]), "spss_pinned_alloc");
+    check(spss_frame_async(ctx, mode, buf_[b], len_), "spss_frame_async");
+    check(spss_synchronize(ctx), "spss_synchronize");
+    if (writer_[1 - b].joinable()) writer_[1 - b].join();  // the previous frame goes first
+    FILE *f = file_;
+    float *frame = buf_[b];
+    const long len = len_;
+    writer_[b] = std::thread([f, t, frame, len]() {
+      std::fwrite(&t, sizeof(float), 1, f);
+      std::fwrite(frame, sizeof(float), (size_t) len, f);
+    });
+    next_ = 1 - b;
+  }
+  void WriteHost(const float *frame, float t)
+  {
+    Flush();
+    std::fwrite(&t, sizeof(float), 1, file_);
+    std::fwrite(frame, sizeof(float), (size_t) len_, file_);
+  }
 
  private:
-  int n_, s_;
-  std::vector<Real> acc_;
-  int count_ = 0;
+  FILE *file_ = nullptr;
+  long len_;
+  int next_ = 0;
+  float *buf_[2] = {nullptr, nullptr};
+  std::thread writer_[2];
 };
 
-// Order parameter of BinaryObserver*::SaveSummaryStatistics
-// (BinaryObserverFirstOrder.cpp:125-142, BinaryObserverSecondOrder.cpp:121-138),
-// accumulated in complex<float> as the reference does; phase index 2 (first
-// order) or 4 (second order).  Writes "t \t |R| \t arg R" lines and, on the
-// observer's cadence, float frames [t][state] of SaveSystemState.
-class BinaryObserver
+// |<e^{i phi}>| and its argument.  A GPU-mirrored state is reduced on the GPU
+// (spss_order_parameters), a host array here; both accumulate in FP64 (the
+// reference accumulates complex<float>, BinaryObserverSecondOrder.cpp:181-188).
+inline void order_parameter(const Real *x, int n, int s, double &abs_r, double &arg_r)
+{
+  if (spss_ctx *ctx = resident(x))
+  {
+    double r[4];
+    check(spss_order_parameters(ctx, r), "SaveSummaryStatistics");
+    abs_r = r[0];
+    arg_r = r[1];
+    return;
+  }
+  const int ip = s == 4 ? 2 : 4;
+  double re = 0.0, im = 0.0;
+  for (int i = 0; i < n; ++i)
+  {
+    re += std::cos(x[(long) s * i + ip]);
+    im += std::sin(x[(long) s * i + ip]);
+  }
+  re /= n;
+  im /= n;
+  abs_r = std::sqrt(re * re + im * im);
+  arg_r = std::atan2(im, re);
+}
+
+}  // namespace detail
+}  // namespace spss
+
+namespace spss
+{
+namespace detail
+{
+
+// Shared body of the four reference binary observers: the two output files,
+// the save cadence (output_time_threshold_) and the progress line.
+class BinaryObserverBase
+{
+ protected:
+  BinaryObserverBase(PeriodicBoundaryConditions &pbc, int n, int s, int threshold, bool wrapped,
+                     const std::string &simulation_file_name, const std::string &summary_file_name)
+      : pbc_(pbc), n_(n), s_(s), threshold_(threshold), wrapped_(wrapped),
+        frames_(simulation_file_name, (long) n * s), timer_(std::chrono::system_clock::now())
+  {
+    std::remove(summary_file_name.c_str());
+    summary_.open(summary_file_name, std::ios::out | std::ios::app);
+    if (!summary_.is_open()) throw Error(SPSS_ERR_INVALID_ARGUMENT, ("cannot open " + summary_file_name).c_str());
+  }
+
+  void ProgressLine(Real t)
+  {
+    const std::chrono::duration<Real> elapsed = std::chrono::system_clock::now() - timer_;
+    if (observer_progress_lines())
+      std::cout << "value at t = " << t << " integrated in " << elapsed.count() << "s" << std::endl;
+    timer_ = std::chrono::system_clock::now();
+  }
+
+  // One frame: BinaryObserverFirstOrder::SaveSystemState (BinaryObserverFirstOrder.cpp:110-120: float
+  // state, positions wrapped into the box and the phase into [0, 2 pi), each wrap evaluated in double on
+  // the float and rounded back) or BinaryObserverSecondOrder::SaveSystemState
+  // (BinaryObserverSecondOrder.cpp:111-116: the float state).
+  void Frame(const Real *x, Real t)
+  {
+    const float tf = (float) t;
+    spss_ctx *ctx = resident(x);
+    const bool unit_box = pbc_.GetXSize() == 1.0 && pbc_.GetYSize() == 1.0;
+    if (ctx && (unit_box || !wrapped_))
+    {
+      frames_.WriteDevice(ctx, wrapped_ ? SPSS_FRAME_WRAPPED : SPSS_FRAME_RAW, tf);
+      return;
+    }
+    host_frame_.assign(x, x + (size_t) n_ * s_);
+    if (wrapped_)
+    {
+      pbc_.ApplyPeriodicBoundaryConditions(host_frame_);
+      for (int i = 0; i < n_; ++i)
+        host_frame_[(size_t) s_ * i + 2] -= std::floor(host_frame_[(size_t) s_ * i + 2] / kTwoPi) * kTwoPi;
+    }
+    frames_.WriteHost(host_frame_.data(), tf);
+  }
+
+  // One summary line "t \t |R| \t arg R" (BinaryObserverFirstOrder.cpp:125-142).
+  void Summary(const Real *x, Real t)
+  {
+    double abs_r, arg_r;
+    order_parameter(x, n_, s_, abs_r, arg_r);
+    summary_ << (float) t << '\t' << (float) abs_r << '\t' << (float) arg_r << std::endl;
+  }
+
+  PeriodicBoundaryConditions &pbc_;
+  int n_, s_;
+  int threshold_;
+  bool wrapped_;
+  FrameFile frames_;
+  std::ofstream summary_;
+  std::vector<float> host_frame_;
+  std::chrono::time_point<std::chrono::system_clock> timer_;
+  int counter_[2] = {0, 0};
+};
+
+}  // namespace detail
+}  // namespace spss
+
+// BinaryObserverFirstOrder (Observers/BinaryObserverFirstOrder.hpp:18-50, .cpp:18-147): every 100th call
+// writes a wrapped float frame and a summary line, to files named after the parameters.
+class BinaryObserverFirstOrder : public spss::detail::BinaryObserverBase
 {
  public:
-  BinaryObserver(int number_of_particles, int number_of_state_variables, const std::string &trajectory_file,
-                 const std::string &summary_file, int every = 10)
-      : n_(number_of_particles), s_(number_of_state_variables), every_(every)
+  BinaryObserverFirstOrder(Thread *, Real v_0, Real xi, Real sigma, Real rho, Real alpha, Real D_phi,
+                           PeriodicBoundaryConditions &pbc_config, int number_of_particles,
+                           int number_of_state_variables, Real, int trial)
+      : BinaryObserverBase(pbc_config, number_of_particles, number_of_state_variables, 100, true,
+                           Name(v_0, xi, sigma, rho, alpha, D_phi, number_of_particles, trial, true),
+                           Name(v_0, xi, sigma, rho, alpha, D_phi, number_of_particles, trial, false))
+  {}
+  void SaveSystemState(const std::vector<Real> &system_state, Real t)
   {
-    if (!trajectory_file.empty()) traj_ = std::fopen(trajectory_file.c_str(), "wb");
-    if (!summary_file.empty()) summ_ = std::fopen(summary_file.c_str(), "w");
-  }
-  ~BinaryObserver()
-  {
-    if (traj_) std::fclose(traj_);
-    if (summ_) std::fclose(summ_);
-  }
-  std::complex<float> OrderParameter(const Real *x) const
-  {
-    const int ip = s_ == 4 ? 2 : 4;
-    std::complex<float> r(0.0f, 0.0f);
-    for (int i = 0; i < n_; ++i) r += std::complex<float>((float) std::cos(x[s_ * i + ip]), (float) std::sin(x[s_ * i + ip]));
-    return r / (float) n_;
-  }
-  void SaveSystemState(const Real *x, Real t)
-  {
-    if (traj_ && !(counter_[0] % every_))
+    if (!(counter_[0] % threshold_))
     {
-      float tf = (float) t;
-      std::vector<float> frame(x, x + (size_t) n_ * s_);
-      std::fwrite(&tf, sizeof(float), 1, traj_);
-      std::fwrite(frame.data(), sizeof(float), frame.size(), traj_);
+      ProgressLine(t);
+      Frame(system_state.data(), t);
     }
     ++counter_[0];
   }
-  void SaveSummaryStatistics(const Real *x, Real t)
+  void SaveSummaryStatistics(const std::vector<Real> &system_state, Real t)
   {
-    if (summ_ && !(counter_[1] % every_))
-    {
-      std::complex<float> r = OrderParameter(x);
-      std::fprintf(summ_, "%g\t%g\t%g\n", (float) t, std::abs(r), std::arg(r));
-    }
+    if (!(counter_[1] % threshold_)) Summary(system_state.data(), t);
     ++counter_[1];
   }
+  void operator()(const std::vector<Real> &system_state, Real t)
+  {
+    SaveSystemState(system_state, t);
+    SaveSummaryStatistics(system_state, t);
+  }
+  // File names of BinaryObserverFirstOrder.cpp:50-76 (the trajectory's alpha onwards at 10 digits).
+  static std::string Name(Real v_0, Real xi, Real sigma, Real rho, Real alpha, Real D_phi, int n, int trial,
+                          bool trajectory)
+  {
+    std::ostringstream b;
+    b << spss::output_folder() << "v0_" << v_0 << "_xi_" << xi << "_sigma_" << sigma << "_rho_" << rho << "_alpha_";
+    if (trajectory) b << std::setprecision(10);
+    b << alpha << "_Dphi_" << D_phi << "_N_" << n << "_" << 0 << "_" << trial << (trajectory ? ".bin" : ".txt");
+    return b.str();
+  }
+};
+
+// BinaryObserverFirstOrderPtr (Observers/BinaryObserverFirstOrderPtr.hpp:18-51, .cpp:20-147): as the serial
+// observer; the progress line comes on every SaveSystemState call.
+class BinaryObserverFirstOrderPtr : public spss::detail::BinaryObserverBase
+{
+ public:
+  BinaryObserverFirstOrderPtr(ThreadSharedMemory *, Real v_0, Real xi, Real sigma, Real rho, Real alpha, Real D_phi,
+                              PeriodicBoundaryConditions &pbc_config, int number_of_particles,
+                              int number_of_state_variables, Real, int trial)
+      : BinaryObserverBase(pbc_config, number_of_particles, number_of_state_variables, 100, true,
+                           Name(v_0, xi, sigma, rho, alpha, D_phi, number_of_particles, trial, ".bin"),
+                           Name(v_0, xi, sigma, rho, alpha, D_phi, number_of_particles, trial, ".txt"))
+  {}
+  void SaveSystemState(Real *const system_state, long, Real t)
+  {
+    ProgressLine(t);
+    if (!(counter_[0] % threshold_)) Frame(system_state, t);
+    ++counter_[0];
+  }
+  void SaveSummaryStatistics(const Real *const system_state, long, Real t)
+  {
+    if (!(counter_[1] % threshold_)) Summary(system_state, t);
+    ++counter_[1];
+  }
+  // File names of BinaryObserverFirstOrderPtr.cpp:52-70.
+  static std::string Name(Real v_0, Real xi, Real sigma, Real rho, Real alpha, Real D_phi, int n, int trial,
+                          const char *ext)
+  {
+    std::ostringstream b;
+    b << spss::output_folder() << "v0_" << v_0 << "_xi_" << xi << "_sigma_" << sigma << "_rho_" << rho << "_alpha_"
+      << alpha << "_Dphi_" << D_phi << "_N_" << n << "_" << 0 << "_" << trial << ext;
+    return b.str();
+  }
+};
+
+// Trajectory and summary file names of BinaryObserverSecondOrder.cpp:50-80 and
+// BinaryObserverSecondOrderPtr.cpp:51-69.
+inline std::string SecondOrderObserverName(Real v_0, Real xi_r, Real D_r, Real xi_phi, Real D_phi, Real sigma,
+                                           Real rho, Real alpha, int n, int trial, bool trajectory)
+{
+  std::ostringstream b;
+  b << spss::output_folder() << (trajectory ? "" : "summary_statistics_") << "v0_" << v_0 << "_xir_" << xi_r
+    << "_Dr_" << D_r << "_xiphi_" << xi_phi << "_Dphi_" << D_phi << "_sigma_" << sigma << "_rho_" << rho
+    << "_alpha_" << alpha << "_N_" << n << "_" << 0 << "_" << trial << (trajectory ? ".bin" : ".txt");
+  return b.str();
+}
+
+// BinaryObserverSecondOrder (Observers/BinaryObserverSecondOrder.hpp:16-55, .cpp:14-138): every 10th call
+// writes the float state and a summary line.
+class BinaryObserverSecondOrder : public spss::detail::BinaryObserverBase
+{
+ public:
+  BinaryObserverSecondOrder(Thread *, Real v_0, Real xi_r, Real D_r, Real xi_phi, Real D_phi, Real sigma, Real rho,
+                            Real alpha, PeriodicBoundaryConditions &pbc_config, int number_of_particles,
+                            int number_of_state_variables, Real, int trial)
+      : BinaryObserverBase(pbc_config, number_of_particles, number_of_state_variables, 10, false,
+                           SecondOrderObserverName(v_0, xi_r, D_r, xi_phi, D_phi, sigma, rho, alpha,
+                                                   number_of_particles, trial, true),
+                           SecondOrderObserverName(v_0, xi_r, D_r, xi_phi, D_phi, sigma, rho, alpha,
+                                                   number_of_particles, trial, false))
+  {}
+  void SaveSystemState(std::vector<Real> &system_state, Real t)
+  {
+    if (!(counter_[0] % threshold_))
+    {
+      ProgressLine(t);
+      Frame(system_state.data(), t);
+    }
+    ++counter_[0];
+  }
+  void SaveSummaryStatistics(std::vector<Real> &system_state, Real t)
+  {
+    if (!(counter_[1] % threshold_)) Summary(system_state.data(), t);
+    ++counter_[1];
+  }
+};
+
+// BinaryObserverSecondOrderPtr (Observers/BinaryObserverSecondOrderPtr.hpp:16-57, .cpp:15-196).
+class BinaryObserverSecondOrderPtr : public spss::detail::BinaryObserverBase
+{
+ public:
+  BinaryObserverSecondOrderPtr(ThreadSharedMemory *, Real v_0, Real xi_r, Real D_r, Real xi_phi, Real D_phi,
+                               Real sigma, Real rho, Real alpha, PeriodicBoundaryConditions &pbc_config,
+                               int number_of_particles, int number_of_state_variables, Real, int trial)
+      : BinaryObserverBase(pbc_config, number_of_particles, number_of_state_variables, 10, false,
+                           SecondOrderObserverName(v_0, xi_r, D_r, xi_phi, D_phi, sigma, rho, alpha,
+                                                   number_of_particles, trial, true),
+                           SecondOrderObserverName(v_0, xi_r, D_r, xi_phi, D_phi, sigma, rho, alpha,
+                                                   number_of_particles, trial, false))
+  {}
+  void SaveSystemState(Real *const system_state, long, Real t)
+  {
+    if (!(counter_[0] % threshold_))
+    {
+      ProgressLine(t);
+      Frame(system_state, t);
+    }
+    ++counter_[0];
+  }
+  void SaveSummaryStatistics(const Real *const system_state, long, Real t)
+  {
+    if (!(counter_[1] % threshold_)) Summary(system_state, t);
+    ++counter_[1];
+  }
+};
+
+namespace spss
+{
+namespace detail
+{
+
+// Shared body of AveragingObserver[Ptr]: the running sum of the state
+// (AveragingObserver.cpp:29-37).  Calls on a GPU-mirrored state add the GPU
+// copy on the GPU (spss_average_accumulate, FP64) into the accumulator of the
+// system that stepped it; other calls add the host array here.  One averaging
+// observer at a time uses a system's accumulator (another one sums on the
+// host); a system destroyed before the average is saved hands its sums over
+// first.
+class AveragingObserverBase
+{
+ protected:
+  AveragingObserverBase(int n, int s) : n_(n), s_(s), sum_((size_t) n * s, 0.0)
+  {
+    listener_ = add_context_listener([this](spss_ctx *ctx) {
+      if (ctx == dev_) Fold();
+    });
+  }
+  ~AveragingObserverBase()
+  {
+    remove_context_listener(listener_);
+    if (dev_) Release(dev_);
+  }
+  AveragingObserverBase(const AveragingObserverBase &) = delete;
+  AveragingObserverBase &operator=(const AveragingObserverBase &) = delete;
+
+  void Accumulate(const Real *x)
+  {
+    spss_ctx *ctx = resident(x);
+    if (ctx && ctx != dev_)
+    {
+      Fold();
+      if (Claim(ctx)) Attach(ctx);
+    }
+    if (ctx && ctx == dev_)
+    {
+      check(spss_average_accumulate(ctx), "AveragingObserver");
+    } else
+    {
+      for (size_t q = 0; q < sum_.size(); ++q) sum_[q] += x[q];
+    }
+    ++count_;
+  }
+
+  // AveragingObserver::SaveAveragedSystemState (AveragingObserver.cpp:39-68): the averaged omega
+  // (component 3) of every particle as float, to a file named after the parameters.
+  void Save(Real v_0, Real xi, Real sigma, Real rho, Real alpha, Real D_phi, int trial)
+  {
+    Fold();
+    std::ostringstream b;
+    b << output_folder() << "averaged_angular_velocities_v0_" << v_0 << "_xi_" << xi << "_sigma_" << sigma
+      << "_rho_" << rho << "_alpha_" << std::setprecision(10) << alpha << "_Dphi_" << D_phi << "_N_" << n_ << "_"
+      << trial << ".bin";
+    std::ofstream file(b.str(), std::ios::out | std::ios::trunc | std::ios::binary);
+    if (!file.is_open()) throw Error(SPSS_ERR_INVALID_ARGUMENT, ("cannot open " + b.str()).c_str());
+    std::vector<RealOutput> w((size_t) n_);
+    for (int i = 0; i < n_; ++i) w[i] = sum_[(size_t) s_ * i + 3] / count_;
+    file.write((const char *) w.data(), n_ * sizeof(RealOutput));
+  }
+
+ public:
+  // Sum of the states accumulated so far (host and GPU calls) and their number.
+  const std::vector<Real> &AccumulatedSystemState()
+  {
+    Fold();
+    return sum_;
+  }
+  int NumberOfAccumulatedSteps() const { return count_; }
 
  private:
-  int n_, s_, every_;
-  int counter_[2] = {0, 0};
-  FILE *traj_ = nullptr;
-  FILE *summ_ = nullptr;
+  static std::vector<spss_ctx *> &claimed()
+  {
+    static std::vector<spss_ctx *> c;
+    return c;
+  }
+  static bool Claim(spss_ctx *ctx)
+  {
+    std::lock_guard<std::mutex> lock(resident_mutex());
+    auto &c = claimed();
+    if (std::find(c.begin(), c.end(), ctx) != c.end()) return false;
+    c.push_back(ctx);
+    return true;
+  }
+  static void Release(spss_ctx *ctx)
+  {
+    std::lock_guard<std::mutex> lock(resident_mutex());
+    auto &c = claimed();
+    c.erase(std::remove(c.begin(), c.end(), ctx), c.end());
+  }
+  // The GPU accumulator's current sums and count.
+  void DeviceSums(spss_ctx *ctx, std::vector<Real> &sums, int &count)
+  {
+    sums.resize(sum_.size());
+    check(spss_average_get(ctx, sums.data(), (long) sums.size(), &count), "AveragingObserver");
+    for (Real &v : sums) v *= count;
+  }
+  void Attach(spss_ctx *ctx)
+  {
+    dev_ = ctx;
+    DeviceSums(ctx, base_, base_count_);
+  }
+  // Move what this observer added on the GPU since Attach into the host sums.
+  void Fold()
+  {
+    if (!dev_) return;
+    std::vector<Real> now;
+    int count = 0;
+    DeviceSums(dev_, now, count);
+    if (count > base_count_)
+      for (size_t q = 0; q < sum_.size(); ++q) sum_[q] += now[q] - base_[q];
+    Release(dev_);
+    dev_ = nullptr;
+  }
+
+  int n_, s_;
+  std::vector<Real> sum_, base_;
+  int count_ = 0, base_count_ = 0;
+  spss_ctx *dev_ = nullptr;
+  int listener_ = 0;
+};
+
+}  // namespace detail
+}  // namespace spss
+
+// AveragingObserver (Observers/AveragingObserver.hpp:12-35, .cpp:13-68).
+class AveragingObserver : public spss::detail::AveragingObserverBase
+{
+ public:
+  AveragingObserver(int number_of_particles, int number_of_state_variables)
+      : AveragingObserverBase(number_of_particles, number_of_state_variables)
+  {}
+  void operator()(const std::vector<Real> &system_state, Real) { Accumulate(system_state.data()); }
+  void SaveAveragedSystemState(Real v_0, Real xi, Real sigma, Real rho, Real alpha, Real D_phi, int trial)
+  {
+    Save(v_0, xi, sigma, rho, alpha, D_phi, trial);
+  }
+};
+
+// AveragingObserverPtr (Observers/AveragingObserverPtr.hpp:14-37, .cpp:13-78).
+class AveragingObserverPtr : public spss::detail::AveragingObserverBase
+{
+ public:
+  AveragingObserverPtr(ThreadSharedMemory *, int number_of_particles, int number_of_state_variables)
+      : AveragingObserverBase(number_of_particles, number_of_state_variables)
+  {}
+  void operator()(Real *const system_state, long, Real) { Accumulate(system_state); }
+  void SaveAveragedSystemState(Real v_0, Real xi, Real sigma, Real rho, Real alpha, Real D_phi, int trial)
+  {
+    Save(v_0, xi, sigma, rho, alpha, D_phi, trial);
+  }
 };
 
 namespace spss
 {
 
-// Binary observer on the GPU state of a system: frames in the reference's
-// .bin format ([float t][float s*n]) computed on the GPU (spss_frame_async)
-// into page-locked buffers and written by a background thread while the next
-// steps run; optional summary lines (t, |R|, arg R).  `wrapped` follows
-// BinaryObserverFirstOrder (positions and phases wrapped), otherwise
-// BinaryObserverSecondOrder (the state as it is).  No counterpart in the
-// reference beyond the file formats.
+// Binary observer on the GPU state of one system, at a cadence of the
+// caller's choice and with file names of the caller's choice: frames in the
+// reference's .bin format computed on the GPU, written by a background thread
+// while the next steps run; optional summary lines (t, |R|, arg R).
+// `wrapped` follows BinaryObserverFirstOrder (positions and phases wrapped),
+// otherwise BinaryObserverSecondOrder (the state as it is).  No counterpart in
+// the reference beyond the file formats.
 class TrajectoryWriter
 {
  public:
   TrajectoryWriter(spss::SystemBase &system, int number_of_particles, int number_of_state_variables,
                    const std::string &trajectory_file, const std::string &summary_file, int every, bool wrapped)
-      : ctx_(system.context()), len_((long) number_of_particles * number_of_state_variables), every_(every),
-        mode_(wrapped ? SPSS_FRAME_WRAPPED : SPSS_FRAME_RAW)
+      : ctx_(system.context()), every_(every), mode_(wrapped ? SPSS_FRAME_WRAPPED : SPSS_FRAME_RAW),
+        frames_(trajectory_file, (long) number_of_particles * number_of_state_variables)
   {
-    traj_ = std::fopen(trajectory_file.c_str(), "wb");
-    if (!traj_) throw std::runtime_error("TrajectoryWriter: cannot open " + trajectory_file);
     if (!summary_file.empty()) summ_ = std::fopen(summary_file.c_str(), "w");
-    for (int b = 0; b < 2; ++b)
-      spss::check(spss_pinned_alloc(sizeof(float) * (size_t) len_, (void **) &buf_[b]), "spss_pinned_alloc");
   }
   TrajectoryWriter(const TrajectoryWriter &) = delete;
   TrajectoryWriter &operator=(const TrajectoryWriter &) = delete;
   ~TrajectoryWriter()
   {
-    for (auto &w : writer_)
-      if (w.joinable()) w.join();
-    for (float *b : buf_)
-      if (b) spss_pinned_free(b);
-    if (traj_) std::fclose(traj_);
+    frames_.Flush();
     if (summ_) std::fclose(summ_);
   }
   void operator()(Real t)
   {
     if (!(counter_++ % every_))
     {
-      const int b = next_;
-      if (writer_[b].joinable()) writer_[b].join();  // this buffer's previous frame is on disk
-      spss::check(spss_frame_async(ctx_, mode_, buf_[b], len_), "spss_frame_async");
+      frames_.WriteDevice(ctx_, mode_, (float) t);
       if (summ_)
       {
         double r[4];
-        spss::check(spss_order_parameters(ctx_, r), "spss_order_parameters");  // synchronises the stream
+        spss::check(spss_order_parameters(ctx_, r), "spss_order_parameters");
         std::fprintf(summ_, "%g\t%g\t%g\n", (float) t, (float) r[0], (float) r[1]);
-      } else
-      {
-        spss::check(spss_synchronize(ctx_), "spss_synchronize");
       }
-      // frames reach the file in order: the previous frame's writer finishes first
-      if (writer_[1 - b].joinable()) writer_[1 - b].join();
-      const float tf = (float) t;
-      float *frame = buf_[b];
-      FILE *f = traj_;
-      const long len = len_;
-      writer_[b] = std::thread([f, tf, frame, len]() {
-        std::fwrite(&tf, sizeof(float), 1, f);
-        std::fwrite(frame, sizeof(float), (size_t) len, f);
-      });
-      next_ = 1 - b;
     }
   }
 
  private:
   spss_ctx *ctx_;
-  long len_;
   int every_, mode_;
-  int counter_ = 0, next_ = 0;
-  float *buf_[2] = {nullptr, nullptr};
-  std::thread writer_[2];
-  FILE *traj_ = nullptr;
+  int counter_ = 0;
+  detail::FrameFile frames_;
   FILE *summ_ = nullptr;
 };
 

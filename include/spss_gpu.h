@@ -93,6 +93,11 @@ int spss_calculate_max_displacement(spss_ctx *ctx, const double *total_displacem
 int spss_get_verlet_state(spss_ctx *ctx, double *accumulated_displacement, int *should_update_lists,
                           int *uses_verlet_list);
 int spss_set_should_update_lists(spss_ctx *ctx, int flag);
+/* Number of list builds the context has performed (Verlet lists, and on the
+ * GB300 path also the per-step cell re-sorts of cell-list contexts): the
+ * rebuilds the trigger above caused.  No reference counterpart (the
+ * reference rebuilds silently). */
+int spss_get_rebuild_count(spss_ctx *ctx, unsigned long long *count);
 
 /* Lists of the most recent build, reference order (pre_linked_list_,
  * linked_list_, verlet_list_; ParticleSystemFirstOrder.hpp:59-66).
@@ -200,7 +205,9 @@ int spss_get_timing(spss_ctx *ctx, double *kernel_ms, unsigned long long *timed_
  * until the process exits and shared by all calls: calls that overlap on the
  * GPU race on it; each call rewrites every partial it reads, so nothing needs
  * clearing between calls.  The first call on a device looks up the array's
- * device address, so make that first call before any stream capture.  Returns
+ * device address, so make that first call before any stream capture.  The
+ * address is kept until the process exits: after cudaDeviceReset on a device
+ * it is stale, so do not call this entry point on that device again.  Returns
  * SPSS_ERR_SIZE for n <= 0 or n > SPSS_NOALLOC_MAX_PARTICLES. */
 int spss_order_parameters_noalloc(int model, const double *state, long n, double *out4, void *cuda_stream);
 

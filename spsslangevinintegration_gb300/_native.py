@@ -72,6 +72,7 @@ SIGNATURES = {
     "spss_calculate_max_displacement": (_i, [_vp, _dp, _l]),
     "spss_get_verlet_state": (_i, [_vp, _dp, _ip, _ip]),
     "spss_set_should_update_lists": (_i, [_vp, _i]),
+    "spss_get_rebuild_count": (_i, [_vp, ctypes.POINTER(ctypes.c_ulonglong)]),
     "spss_get_pre_linked_list": (_i, [_vp, _ip, _l]),
     "spss_get_cells": (_i, [_vp, _ip, _l, _ip, _l, _ip]),
     "spss_get_verlet_lists": (_i, [_vp, _ip, _l, _ip, _l, P(_l)]),

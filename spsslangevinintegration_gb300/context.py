@@ -15,23 +15,17 @@ def make_params(model, n, rho, precision=N.PRECISION_F64, variant=N.VARIANT_DISP
                     rho, alpha, r_max, seed, replica)
 
 
-class PinnedArray:
-    """A page-locked, device-mapped host array (spss_pinned_alloc).  Passed to
-    Context.step_host, the upload and download kernels read and write it over
-    the host link directly (no registration, no staging copy); the observers'
-    frame buffers are of this kind too."""
+class _PinnedAllocation:
+    """Owner of one spss_pinned_alloc block; freed when the last reference
+    (a PinnedArray or any numpy view of its memory) goes away."""
 
-    def __init__(self, count, dtype=np.float64):
-        dtype = np.dtype(dtype)
+    def __init__(self, nbytes):
         ptr = ctypes.c_void_p()
-        N.check(N.lib().spss_pinned_alloc(int(count) * dtype.itemsize, ctypes.byref(ptr)), "spss_pinned_alloc")
+        N.check(N.lib().spss_pinned_alloc(int(nbytes), ctypes.byref(ptr)), "spss_pinned_alloc")
         self.ptr = ptr
-        raw = (ctypes.c_char * (int(count) * dtype.itemsize)).from_address(ptr.value)
-        self.array = np.frombuffer(raw, dtype=dtype, count=int(count))
 
     def free(self):
-        if getattr(self, "ptr", None):
-            self.array = None
+        if self.ptr:
             N.lib().spss_pinned_free(self.ptr)
             self.ptr = None
 
@@ -40,6 +34,33 @@ class PinnedArray:
             self.free()
         except Exception:
             pass
+
+
+class PinnedArray:
+    """A page-locked, device-mapped host array (spss_pinned_alloc).  Passed to
+    Context.step_host, the upload and download kernels read and write it over
+    the host link directly (no registration, no staging copy); the observers'
+    frame buffers are of this kind too.  The memory lives as long as the
+    PinnedArray or any numpy view of `array` does (the views hold the
+    allocation); `free()` releases it at once, after which existing views
+    must not be used."""
+
+    def __init__(self, count, dtype=np.float64):
+        dtype = np.dtype(dtype)
+        nbytes = int(count) * dtype.itemsize
+        self._alloc = _PinnedAllocation(nbytes)
+        raw = (ctypes.c_char * nbytes).from_address(self._alloc.ptr.value)
+        raw._owner = self._alloc  # numpy views keep `raw`, and `raw` keeps the allocation
+        self.array = np.frombuffer(raw, dtype=dtype, count=int(count))
+
+    @property
+    def ptr(self):
+        return self._alloc.ptr
+
+    def free(self):
+        if getattr(self, "_alloc", None) is not None:
+            self.array = None
+            self._alloc.free()
 
     def __enter__(self):
         return self
@@ -130,6 +151,13 @@ class Context:
 
     def set_should_update_lists(self, flag):
         N.check(self.L.spss_set_should_update_lists(self.h, int(flag)), "spss_set_should_update_lists")
+
+    @property
+    def rebuild_count(self):
+        """List builds performed so far (spss_get_rebuild_count)."""
+        c = ctypes.c_ulonglong()
+        N.check(self.L.spss_get_rebuild_count(self.h, ctypes.byref(c)), "spss_get_rebuild_count")
+        return c.value
 
     # -- lists
     def pre_linked_list(self):

@@ -722,6 +722,7 @@ int f64_evaluate(spss_ctx *ctx, int variant, const double *d_state, const double
       {
         SPSS_TRY(build_verlet(ctx, k, variant == SPSS_VARIANT_LINKED_LIST_VERLET));
         ctx->should_update_lists = 0;
+        ++ctx->list_builds;
       }
       ctx->uses_verlet_list = 1;
       f64_verlet_pairs_kernel<<<blocks_for(k.n, 128), 128, 0, ctx->stream>>>(k, f->rk.ptr, f->vl_off.ptr,

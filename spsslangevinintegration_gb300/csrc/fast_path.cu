@@ -197,6 +197,10 @@ struct FastPath
   FastControl *ctrl = nullptr;    // device
   FastControl *h_ctrl = nullptr;  // pinned mirror
   int kind = KIND_CELLS;
+  // Verlet bookkeeping without lists: a Verlet-list context whose radius
+  // leaves fewer than three cells per side evaluates all pairs every step and
+  // keeps the displacement trigger (uses_verlet_list, accumulated displacement).
+  bool trigger_only = false;
   int nc_build = 1;
   int cap = 0;
   bool have_state = false;
@@ -2157,10 +2161,18 @@ int fast_create(spss_ctx *ctx)
         grid = nc;
         break;
       case SPSS_VARIANT_VERLET:
-        // O(N^2) list build = every pair within r_max: cells no smaller than r_max
-        k = KIND_VERLET;
+        // O(N^2) list build = every pair within r_max: cells no smaller than r_max.  With fewer
+        // than three such cells per side (r_max > 1/3: the reference's first-order dispatch for
+        // 0.25 < rho <= 0.5, ParticleSystemFirstOrder.cpp:96-111) a list holds a third of the
+        // system or more and the stencil would visit cells twice: every pair is evaluated each
+        // step instead, the same neighbours within rho, with the list trigger kept.
         grid = std::max(1, (int) (1.0 / r_max));
-        if (grid < 3) return SPSS_ERR_NOT_SUPPORTED;
+        k = grid < 3 ? KIND_ALL_PAIRS : KIND_VERLET;
+        if (grid < 3)
+        {
+          grid = 1;
+          f->trigger_only = true;
+        }
         break;
       case SPSS_VARIANT_LINKED_LIST_VERLET:
         k = KIND_VERLET;
@@ -2194,7 +2206,7 @@ int fast_create(spss_ctx *ctx)
     SPSS_CUDA_TRY(cudaMemsetAsync(f->nu.ptr, 0, sizeof(float) * n, ctx->stream));
   }
   f->nc_build = f->h_sys[0].nc;
-  if (f->kind == KIND_VERLET) ctx->uses_verlet_list = 1;
+  if (f->kind == KIND_VERLET || f->trigger_only) ctx->uses_verlet_list = 1;
   for (int b = 0; b < 2; ++b)
   {
     SPSS_TRY(f->rec[b].reserve(n));
@@ -2419,7 +2431,7 @@ static int launch_step(spss_ctx *ctx, int stepper, const FastParams &P)
   if (ctx->timing) SPSS_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
   FastPath *f = ctx->fast;
   fast_control_kernel<<<1, 256, 0, ctx->stream>>>(f->ctrl, f->sysctl.ptr, f->sys.ptr, f->nsys, P.always_rebuild,
-                                                   f->kind == KIND_VERLET);
+                                                   f->kind == KIND_VERLET || f->trigger_only);
   ++ctx->launches;
   return check_launch("fast_control_kernel");
 }
@@ -2671,6 +2683,13 @@ int fast_system_order_parameters(spss_ctx *ctx, double *h_out)
   SPSS_CUDA_TRY(cudaMemcpyAsync(h_out, f->order_out.ptr, sizeof(double) * 4 * f->nsys, cudaMemcpyDeviceToHost,
                                 ctx->stream));
   SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SPSS_OK;
+}
+
+int fast_rebuild_count(spss_ctx *ctx, unsigned long long *count)
+{
+  SPSS_TRY(sync_control(ctx));
+  *count = (unsigned long long) ctx->fast->h_ctrl->rebuilds;
   return SPSS_OK;
 }
 

@@ -248,9 +248,10 @@ int spss_create(const spss_params *params, spss_ctx **out)
   derive_lists(p, ctx->r_min, ctx->r_max, ctx->nc, ctx->nc_verlet);
   ctx->should_update_lists = 1;
   int rc = SPSS_OK;
-  if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaError_t e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking))
   {
     cudaGetLastError();
+    record_cuda_error(e, "creating the context's stream", __FILE__, __LINE__);
     delete ctx;
     return SPSS_ERR_CUDA;
   }
@@ -389,6 +390,17 @@ int spss_get_verlet_state(spss_ctx *ctx, double *accumulated_displacement, int *
   if (should_update_lists) *should_update_lists = ctx->should_update_lists;
   if (uses_verlet_list) *uses_verlet_list = ctx->uses_verlet_list;
   return SPSS_OK;
+}
+
+int spss_get_rebuild_count(spss_ctx *ctx, unsigned long long *count)
+{
+  if (!ctx || !count) return SPSS_ERR_INVALID_ARGUMENT;
+  if (is_f64(ctx))
+  {
+    *count = ctx->list_builds;
+    return SPSS_OK;
+  }
+  return fast_rebuild_count(ctx, count);
 }
 
 int spss_set_should_update_lists(spss_ctx *ctx, int flag)
@@ -760,9 +772,10 @@ int spss_batch_create(const spss_params *systems, int nsys, spss_ctx **out)
   ctx->s = p0.model == 1 ? 4 : 6;
   derive_lists(p0, ctx->r_min, ctx->r_max, ctx->nc, ctx->nc_verlet);
   ctx->should_update_lists = 1;
-  if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaError_t e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking))
   {
     cudaGetLastError();
+    record_cuda_error(e, "creating the context's stream", __FILE__, __LINE__);
     delete ctx;
     return SPSS_ERR_CUDA;
   }

@@ -276,6 +276,7 @@ struct spss_ctx
   double accumulated_displacement = 0.0;
   int should_update_lists = 1;
   int uses_verlet_list = 0;
+  unsigned long long list_builds = 0;  // Verlet / cell list builds so far (FP64 path; the fast path counts on the device)
   double r_min = 0.0, r_max = 0.0;
   int nc = 1, nc_verlet = 1;
   // host registration of the caller's array for spss_step_host
@@ -317,6 +318,7 @@ int f64_state_ptr(spss_ctx *ctx, const double **d_aos);
 // Fast (GB300) path, fast_path.cu
 int fast_create(spss_ctx *ctx);
 void fast_destroy(spss_ctx *ctx);
+int fast_rebuild_count(spss_ctx *ctx, unsigned long long *count);
 int fast_set_state(spss_ctx *ctx, const double *d_aos);
 int fast_get_state(spss_ctx *ctx, double *d_aos);
 int fast_evaluate(spss_ctx *ctx, int variant, const double *d_state, const double *d_kprev, double *d_knext,

@@ -6,7 +6,8 @@
 //
 // usage: dropin_example <dir>   reads <dir>/fo_init.bin, <dir>/so_init.bin
 //                                writes fo_final.bin, so_final.bin, so_noise.bin,
-//                                fo_traj.bin, fo_summary.txt, fo_restart.bin
+//                                fo_traj.bin, fo_summary.txt, fo_restart.bin,
+//                                {fo,so}_addnoise.bin, {fo,so}_addnoise_z.bin
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -84,6 +85,34 @@ int main(int argc, char **argv)
       }
       write_all(dir + "/so_final.bin", x);
       write_all(dir + "/so_noise.bin", noise);
+
+      // AddNoise (ParticleSystemSecondOrder.cpp:439-451) twice into a derivative buffer; the
+      // normals of the second call recorded
+      std::vector<Real> derivative((size_t) n * s, 7.0), z((size_t) n * 3);
+      system.AddNoise(x, derivative, t);
+      unsigned long long step = 0;
+      spss::check(spss_get_step_counter(system.context(), &step), "spss_get_step_counter");
+      spss::check(spss_noise(system.context(), SPSS_STEPPER_STOCHASTIC_EULER, step, z.data(), (long) z.size()),
+                  "spss_noise");
+      system.AddNoise(x, derivative, t);
+      write_all(dir + "/so_addnoise.bin", derivative);
+      write_all(dir + "/so_addnoise_z.bin", z);
+    }
+    {
+      // first-order AddNoise (ParticleSystemFirstOrder.cpp:698-708): sqrt(2 D_phi) N(0,1) into omega only
+      const int n = 300, s = 4;
+      Thread thread(argc, argv, n, s);
+      PeriodicBoundaryConditions pbc(&thread, n, s, 1.0, 1.0);
+      ParticleSystemFirstOrder system(&thread, 0.3, 0.1, 1.0, 0.1, 0.2, 0.25, pbc, n, s);
+      std::vector<Real> x((size_t) n * s, 0.5), derivative((size_t) n * s, 7.0), z((size_t) n);
+      system.AddNoise(x, derivative, 0.0);
+      unsigned long long step = 0;
+      spss::check(spss_get_step_counter(system.context(), &step), "spss_get_step_counter");
+      spss::check(spss_noise(system.context(), SPSS_STEPPER_STOCHASTIC_EULER, step, z.data(), (long) z.size()),
+                  "spss_noise");
+      system.AddNoise(x, derivative, 0.0);
+      write_all(dir + "/fo_addnoise.bin", derivative);
+      write_all(dir + "/fo_addnoise_z.bin", z);
     }
   } catch (const std::exception &e)
   {

@@ -1,8 +1,8 @@
 """Generate the golden fixtures in this directory from the reference itself.
 
-Run in a tree that holds the reference sources (default /root/reference):
+Run with the path of the reference source tree (or SPSS_REFERENCE set):
 
-    python tests/golden/make_golden.py [--ref /path/to/reference]
+    python tests/golden/make_golden.py --ref /path/to/reference
 
 It compiles the reference's own hot-path sources unmodified (``make ref`` in
 ``oracle/``: single-rank MPI stand-in, noise-replay shim, -ffp-contract=off),
@@ -205,8 +205,11 @@ def run_case(c, tmp):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("SPSS_REFERENCE"),
+                    help="reference source tree (default: $SPSS_REFERENCE)")
     args = ap.parse_args()
+    if not args.ref:
+        ap.error("give the reference source tree with --ref or SPSS_REFERENCE")
     subprocess.run(["make", "-s", "-C", ORACLE, "ref", "REF=" + args.ref], check=True)
     with tempfile.TemporaryDirectory() as tmp:
         for c in CASES:

@@ -4,6 +4,8 @@ import ctypes
 import os
 import re
 
+import pytest
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -76,16 +78,17 @@ def test_batch_argument_checks_without_gpu():
     assert L.spss_autotune(None, 1, 0.005, 2, None) == _native.ERR_INVALID_ARGUMENT
 
 
-def test_cpp_dropin_example_compiles_and_links(tmp_path):
-    """The reference-named C++ classes (include/spss/spss.hpp) and the example
-    program that drives them compile and link against the library without a
-    GPU (running them needs one)."""
+@pytest.mark.parametrize("program", ["dropin_example.cpp", "engine_loops.cpp"])
+def test_cpp_dropin_programs_compile_and_link(tmp_path, program):
+    """The reference-named C++ classes (include/spss/spss.hpp) and the programs
+    that drive them as the reference's engines do compile warning-free and
+    link against the library without a GPU (running them needs one)."""
     import subprocess
 
     lib = built_library()
-    exe = str(tmp_path / "dropin_example")
-    subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-I" + os.path.join(ROOT, "include"),
-                    os.path.join(ROOT, "tests", "cpp", "dropin_example.cpp"), "-o", exe, "-pthread",
+    exe = str(tmp_path / program.replace(".cpp", ""))
+    subprocess.run(["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", program), "-o", exe, "-pthread",
                     "-L" + os.path.dirname(lib), "-lspss_gpu", "-Wl,-rpath," + os.path.dirname(lib)], check=True)
     assert os.path.getsize(exe) > 0
 

@@ -42,3 +42,20 @@ def test_dopri5_observer_can_stop():
         ctx.set_state(initial(1, 200, 3))
         ctx.integrate_dopri5(0.0, 5.0, 0.5, observer=lambda x, t: seen.append(t) or t >= 1.0)
     assert seen == [0.0, 0.5, 1.0]
+
+
+def test_dopri5_on_a_closed_form_solution():
+    """The GPU integrator on uncoupled particles without friction, whose
+    trajectories are known in closed form (tests/test_dopri5_method.py):
+    within 10 x the requested tolerance at every observer time."""
+    from test_dopri5_method import _closed_form, closed_form_case
+
+    p, x0 = closed_form_case()
+    got = []
+    with gpu_context(p, precision=0, variant=1) as ctx:
+        ctx.set_state(x0)
+        ctx.integrate_dopri5(0.0, 3.0, 0.25, 1e-8, 1e-8, observer=lambda x, t: got.append((t, x)))
+    assert len(got) == 13
+    for t, x in got:
+        exact = _closed_form(x0, t, p["v0"])
+        assert np.max(np.abs(x - exact) / (1.0 + np.abs(exact))) <= 1e-7, t

@@ -44,6 +44,8 @@ def test_dropin_classes_match_oracle():
         times, frames = read_frames(os.path.join(d, "fo_traj.bin"), 400, 4)
         summary = np.loadtxt(os.path.join(d, "fo_summary.txt"))
         restart = np.fromfile(os.path.join(d, "fo_restart.bin"))
+        addnoise = {m: (np.fromfile(os.path.join(d, m + "_addnoise.bin")),
+                        np.fromfile(os.path.join(d, m + "_addnoise_z.bin"))) for m in ("fo", "so")}
 
     sysm = ob.System(1, 400, 0.1, v0=0.3, xi=0.1, sigma=1.0, alpha=0.2, D_phi=0.1, flavor=0)
     x, t = fo.copy(), 0.0
@@ -72,3 +74,18 @@ def test_dropin_classes_match_oracle():
         sysm.step(ob.SE, 0, x, t, 0.005, noise[k * 1500:(k + 1) * 1500])
         ob.apply_pbc(2, x)
     per_component_close(so_gpu, x, 6, 1e-11, "second-order SE drop-in")
+
+    # AddNoise writes sqrt(2 D) times the step's normals into the noise
+    # components and leaves the others as they were
+    # (ParticleSystemFirstOrder.cpp:698-708, ParticleSystemSecondOrder.cpp:439-451)
+    d, z = addnoise["fo"]
+    d = d.reshape(300, 4)
+    np.testing.assert_array_equal(d[:, :3], 7.0)
+    np.testing.assert_allclose(d[:, 3], np.sqrt(2.0 * 0.25) * z, rtol=1e-15)
+    assert abs(z.mean()) < 0.2 and 0.8 < z.std() < 1.2
+    d, z = addnoise["so"]
+    d, z = d.reshape(500, 6), z.reshape(500, 3)
+    np.testing.assert_array_equal(d[:, [0, 1, 4]], 7.0)
+    np.testing.assert_allclose(d[:, 2], np.sqrt(2.0 * 0.02) * z[:, 0], rtol=1e-15)
+    np.testing.assert_allclose(d[:, 3], np.sqrt(2.0 * 0.02) * z[:, 1], rtol=1e-15)
+    np.testing.assert_allclose(d[:, 5], np.sqrt(2.0 * 0.1) * z[:, 2], rtol=1e-15)

@@ -322,3 +322,41 @@ def test_global_field_matches_fp64_oracle(stepper):
     ctx.close()
     assert np.quantile(err, 0.999) <= 1e-3
     assert np.median(err) <= 1e-5
+
+
+@pytest.mark.parametrize("stepper", [1, 2])
+@pytest.mark.parametrize("variant", [0, 3])
+def test_verlet_radius_over_a_third_runs_all_pairs_with_the_trigger(variant, stepper):
+    """The reference's first-order dispatch picks the O(N^2) Verlet list for
+    0.25 < rho <= 0.5 (ParticleSystemFirstOrder.cpp:96-111, r_max = rho + 0.05):
+    with r_max > 1/3 the fast path evaluates every pair each step and keeps
+    the list trigger.  One step within 1e-5 of the oracle's Verlet routine
+    (ParticleSystemFirstOrder.cpp:355-477); 20 steps track it with the same
+    rebuild steps and accumulated displacement."""
+    from helpers import gpu_context, oracle_system
+
+    n, rho = 600, 0.3
+    p = dict(model=1, n=n, rho=rho, flavor="ptr", v0=0.5, xi=0.1, sigma=1.0, D_phi=0.1, alpha=0.2)
+    x0 = initial(1, n, 4, omega=0.5)
+    with gpu_context(p, precision=F32, variant=variant, seed=2) as ctx:
+        orc = oracle_system(p)
+        assert ctx.verlet_state()[2] == 1
+        ctx.set_state(x0)
+        x = x0.copy()
+        flags_g, flags_o = [], []
+        for k in range(20):
+            normals = ctx.noise(stepper, k)
+            ctx.step(stepper, (k + 1) * 0.005, 0.005)
+            orc.step(stepper, 3, x, (k + 1) * 0.005, 0.005, normals)
+            acc, flag, uses = ctx.verlet_state()
+            assert uses == 1
+            assert acc == pytest.approx(orc.accumulated_displacement, rel=1e-5, abs=1e-12)
+            flags_g.append(flag)
+            flags_o.append(orc.should_update_lists)
+            if k == 0:
+                assert state_err(ctx.get_state(), x, 4).max() <= 1e-5
+        got = ctx.get_state()
+    assert flags_g == flags_o and any(flags_o)
+    err = state_err(got, x, 4).max(axis=1)
+    assert np.quantile(err, 0.999) <= 1e-3
+    assert np.median(err) <= 1e-5

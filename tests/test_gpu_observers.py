@@ -65,3 +65,23 @@ def test_trajectory_writer_and_restart():
         np.testing.assert_allclose(line[1:], rk[:2].astype(np.float32), rtol=1e-5, atol=1e-7)
     assert t_last == times[-1]
     np.testing.assert_array_equal(x_last, frames[-1].astype(np.float64))
+
+
+def test_pinned_array_view_keeps_its_memory():
+    """A numpy view of a PinnedArray keeps the page-locked block alive after
+    the PinnedArray itself is gone, and the block is freed with the last view."""
+    import gc
+    import weakref
+
+    from spsslangevinintegration_gb300 import PinnedArray
+
+    pa = PinnedArray(4096)
+    owner = weakref.ref(pa._alloc)
+    view = pa.array
+    del pa
+    gc.collect()
+    view[:] = 2.5
+    assert owner() is not None and float(view.sum()) == 2.5 * 4096
+    del view
+    gc.collect()
+    assert owner() is None
