@@ -214,6 +214,94 @@ def cpu_cells_sample(n, budget_s=8.0):
                       "oracle port, OpenMP %d threads" % (n, steps, el, cores)}
 
 
+def config_system(model, n, density, v0, m=1.0, sigma=1.0, D=0.1, xi=0.1):
+    """A physical configuration in the reference's unit box (second order:
+    xi_r = xi_phi = 1/m, sigma/m, D_phi = D/m^2, D_r = 0; first order the
+    reference's friction xi = 0.1, D_phi = D)."""
+    L = np.sqrt(n / density)
+    if model == 1:
+        kw = dict(v0=v0 / L, xi=xi, sigma=sigma, D_phi=D, alpha=0.0)
+    else:
+        kw = dict(v0=v0 / L, xi_r=1.0 / m, xi_phi=1.0 / m, D_r=0.0, D_phi=D / m ** 2, sigma=sigma / m, alpha=0.0)
+    return RADIUS / L, kw, L
+
+
+def first_order_initial(n, seed):
+    rng = np.random.default_rng(seed)
+    x = np.zeros((n, 4))
+    x[:, 0], x[:, 1] = rng.random(n), rng.random(n)
+    x[:, 2] = rng.uniform(-np.pi, np.pi, n)
+    return x.reshape(-1)
+
+
+def run_config_legs(args, rank, world, barrier, max_over_ranks):
+    """The two smaller benchmark configurations next to the oracle port of the
+    same workload on this host's cores:
+      1. first order, N = 1000, density 1, all pairs called directly, RK4,
+         D = 0, v0 = 0.1, sigma = 1, dt = 0.01, FP64 (the reference's
+         arithmetic path), the configuration's 1000 steps;
+      2. second order, N = 65,536, density 2, cell list, StochasticEuler,
+         D = 0.1, m = 1, v0 = 0.5, dt = 0.005, FP32 (GB300 path), 2000 of the
+         configuration's 10,000 steps."""
+    import torch
+
+    from oracle import binding as ob
+    from spsslangevinintegration_gb300 import ALL_PAIRS, LINKED_LIST, PRECISION_F32, PRECISION_F64, RK4, \
+        STOCHASTIC_EULER, Context
+
+    out = {}
+    cores = os.cpu_count() or 1
+    ob.set_threads(cores, bench=True)
+    cases = (("config1", 1, 1000, 1.0, 0.1, 0.0, RK4, ALL_PAIRS, PRECISION_F64, 0.01, 1000, 1000),
+             ("config2", 2, 65536, 2.0, 0.5, 0.1, STOCHASTIC_EULER, LINKED_LIST, PRECISION_F32, DT, 2000, 10000))
+    for name, model, n, density, v0, D, stepper, variant, precision, dt, steps, full in cases:
+        rho, kw, L = config_system(model, n, density, v0, D=D)
+        x0 = first_order_initial(n, rank) if model == 1 else initial_state(n, L, rank)
+        ctx = Context(model, n, rho, precision=precision, variant=variant, flavor=0, seed=12345, replica=rank, **kw)
+        ctx.set_state(x0)
+        ctx.steps(stepper, 0.0, dt, 5)
+        barrier()
+        launches0 = ctx.kernel_launches
+        t0 = time.perf_counter()
+        ctx.steps(stepper, 0.0, dt, steps)
+        ctx.synchronize()
+        barrier()
+        el = max_over_ranks(time.perf_counter() - t0)
+        launches = ctx.kernel_launches - launches0
+        ctx.close()
+        if rank != 0:
+            continue
+        entry = {"workload": "%s order, N=%d, density %g, R=1, %s, %s, dt=%g, %s" % (
+                     "first" if model == 1 else "second", n, density,
+                     "all pairs" if variant == ALL_PAIRS else "cell list",
+                     "RK4, D=0, v0=0.1, sigma=1 (FP64 path)" if model == 1 else
+                     "StochasticEuler, D=0.1, m=1, v0=0.5, sigma=1 (FP32 path)", dt,
+                     "%d of the configuration's %d steps timed" % (steps, full)),
+                 "value": n * steps * world / el, "unit": "particle-steps/s", "ms_per_step": 1e3 * el / steps,
+                 "steps_timed": steps, "gpu_launches_per_step": launches / steps,
+                 "timing": "wall clock around %d steps (graph launches where the path has them, one host "
+                           "synchronisation), max over ranks" % steps}
+        if not args.no_cpu_baseline and world == 1:
+            sysm = ob.System(model, n, rho, flavor=0, bench=True, **kw)
+            x = x0.copy()
+            per = 0 if stepper == RK4 else ob.normals_per_particle(model, stepper)
+            k, c0 = 0, time.perf_counter()
+            while True:
+                normals = ob.philox_normals(0, k, 0, per * n, bench=True) if per else None
+                sysm.step(stepper, variant, x, dt * (k + 1), dt, normals)
+                k += 1
+                cel = time.perf_counter() - c0
+                if cel >= args.cpu_seconds / 4 or k >= steps:
+                    break
+            sysm.close()
+            entry["cpu_baseline"] = {"value": n * k / cel, "unit": "particle-steps/s", "cores": cores,
+                                     "kind": "port", "sample": "%d steps of the same workload (%.1f s), FP64 oracle "
+                                     "port, OpenMP %d threads" % (k, cel, cores)}
+            entry["speedup_vs_cpu"] = entry["value"] / entry["cpu_baseline"]["value"]
+        out[name] = entry
+    return out if rank == 0 else None
+
+
 def run_cells_leg(args, rank, world, barrier, max_over_ranks):
     """The main leg's workload with cell lists rebuilt every step (the
     reference's linked list) instead of Verlet lists, device-timed, next to
@@ -287,23 +375,29 @@ def sweep_cpu_sample(points, budget_s=8.0):
         "OpenMP %d threads, %.1f s" % (kw["n"], steps, cores, el)
 
 
-def run_sweep_leg(args, rank, world, barrier, max_over_ranks):
+def run_sweep_leg(args, rank, world, barrier, max_over_ranks, verlet=False):
     """Batched parameter sweep: 512 independent systems in one batch context
     (one CUDA graph per step for all systems), tiling picked by the autotuner;
-    phase-diagram points per hour at 20,000 steps per point."""
+    phase-diagram points per hour at 20,000 steps per point.  Cell lists
+    rebuilt every step (the configuration's choice), or with `verlet` the
+    reference's linked list + Verlet routine with skin 0.3 R, each system's
+    lists rebuilt when its own displacement trigger fires (the same neighbour
+    sets within R)."""
     import torch
 
-    from spsslangevinintegration_gb300 import STOCHASTIC_EULER, sweep
+    from spsslangevinintegration_gb300 import LINKED_LIST, LINKED_LIST_VERLET, STOCHASTIC_EULER, sweep
     from spsslangevinintegration_gb300.replicas import shard
 
     points = sweep.replica_table(SWEEP_SYSTEMS, seed=0)
     mine = [points[i] for i in shard(len(points), world, rank)]
-    b = sweep.make_batch(mine, seed=0, first_replica=shard(len(points), world, rank)[0])
+    b = sweep.make_batch(mine, seed=0, first_replica=shard(len(points), world, rank)[0],
+                         variant=LINKED_LIST_VERLET if verlet else LINKED_LIST, skin=SKIN if verlet else 0.0)
     b.steps(STOCHASTIC_EULER, 0.0, DT, 3)
     tune_ms = b.autotune(STOCHASTIC_EULER, DT, steps=4)
     b.run(STOCHASTIC_EULER, 0.0, DT, 10, sample_every=SWEEP_SAMPLE_EVERY, sample_from=0)
     steps = max(20, min(args.sweep_steps, 2000))
     launches0 = b.kernel_launches
+    rebuilds0 = b.rebuild_count
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -312,26 +406,29 @@ def run_sweep_leg(args, rank, world, barrier, max_over_ranks):
     barrier()
     el = max_over_ranks(time.perf_counter() - t0)
     launches = b.kernel_launches - launches0
+    rebuild_steps = b.rebuild_count - rebuilds0
     tiling = b.tiling()
     total_n = sum(p["n"] for p in points)
     b.close()
     if rank != 0:
         return None
     s_per_step = el / steps
+    lists = ("linked list + Verlet lists (skin 0.3R), each system rebuilt on its own displacement trigger"
+             if verlet else "cell lists rebuilt every step")
     out = {
         "workload": "%d independent systems (second-order model): N log-uniform in [1024, 65536] (total %d), "
                     "sigma uniform in [0, 3], D log-uniform in [0.01, 1], m in {0.1, 1, 10}, density 2, R=1, "
-                    "v0=0.5, cell lists rebuilt every step, StochasticEuler dt=0.005, per-system time-averaged "
-                    "phase and velocity order parameters sampled every %d steps" % (len(points), total_n,
+                    "v0=0.5, %s, StochasticEuler dt=0.005, per-system time-averaged "
+                    "phase and velocity order parameters sampled every %d steps" % (len(points), total_n, lists,
                                                                                    SWEEP_SAMPLE_EVERY),
         "steps_timed": steps, "ms_per_step": 1e3 * s_per_step, "particle_steps_per_s": total_n / s_per_step,
         "points_per_hour": len(points) * 3600.0 / (SWEEP_STEPS_PER_POINT * s_per_step),
         "points_per_hour_unit": "phase-diagram points per hour at %d steps per point" % SWEEP_STEPS_PER_POINT,
         "tiling": {"tile_cells": tiling[0], "persistent": tiling[1], "autotuned_ms_per_step": tune_ms},
-        "gpu_launches_per_step": launches / steps,
+        "gpu_launches_per_step": launches / steps, "steps_with_a_rebuild": rebuild_steps,
         "timing": "wall clock around %d steps (graph launches, one host synchronisation), max over ranks" % steps,
     }
-    if not args.no_cpu_baseline and world == 1:
+    if not args.no_cpu_baseline and world == 1 and not verlet:
         rate, cores, sample = sweep_cpu_sample(points, budget_s=args.cpu_seconds / 2)
         out["cpu_baseline"] = {"particle_steps_per_s": rate, "cores": cores, "kind": "port", "sample": sample,
                                "points_per_hour": len(points) * 3600.0 * rate / (total_n * SWEEP_STEPS_PER_POINT)}
@@ -342,9 +439,15 @@ def run_surrogate_leg(args):
     """Phase diagram over a 256 x 256 (sigma, D) grid (N = 1024, density 2,
     m = 1, v0 = 0.5, 4000 SE steps per run) from the learned surrogate with one
     active-learning round, checked against a 256-replica reference at 48
-    random grid points; the plain method's cost at the same precision is the
-    measured single-run rate divided by the runs a point needs for a 0.02
-    standard error (from the reference's run-to-run spread)."""
+    random grid points.  The plain method at the same precision is timed on
+    the same workload: R runs at each of 80 grid points (the 48 checked ones
+    and 32 more), R chosen so that a point's mean lands within 0.02 with 95 %
+    probability (R = (1.96 std / 0.02)^2 averaged over the checked points, std
+    the reference's run-to-run spread; the surrogate's own fraction within
+    0.02 is measured at the same points), batched like the surrogate's
+    training runs."""
+    import torch
+
     from spsslangevinintegration_gb300 import surrogate as S
 
     grid = S.grid_points(256, 256)
@@ -356,8 +459,21 @@ def run_surrogate_leg(args):
     err = np.abs(res["values"][idx] - mean).max(axis=1)
     runs_needed = float(np.maximum(1.0, (std.max(axis=1) / 0.02) ** 2).mean())
     single_rate = args.surrogate_train / res["seconds"]["simulate_training"]  # plain runs per second
-    plain_pph = single_rate * 3600.0 / runs_needed
+    derived_pph = single_rate * 3600.0 / runs_needed
     sur_pph = len(grid) * 3600.0 / total
+    # the plain replicated sweep, timed, at 95 % within 0.02
+    reps = int(np.ceil(np.mean(np.maximum(1.0, (1.96 * std.max(axis=1) / 0.02) ** 2))))
+    others = [i for i in np.random.default_rng(12).permutation(len(grid)) if i not in set(idx.tolist())][:32]
+    subset = list(idx) + others
+    torch.cuda.synchronize()
+    p0 = time.perf_counter()
+    runs = S.run_values(S.simulate([grid[i] for i in subset for _ in range(reps)], steps=4000, sample_every=10,
+                                   seed=0, first_replica=2 * 10 ** 7))
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - p0
+    plain_est = runs.reshape(len(subset), reps, 2).mean(axis=1)[:len(idx)]
+    plain_err = np.abs(plain_est - mean).max(axis=1)
+    plain_pph = len(subset) * 3600.0 / plain_s
     z = np.abs(res["judge_z"]).max(axis=1)
     return {
         "workload": "256 x 256 (sigma in [0, 3], D log in [0.01, 1]) phase diagram of the expected phase and "
@@ -366,9 +482,19 @@ def run_surrogate_leg(args):
         "network": "5-128-128-128-4 GELU, BF16 operands, FP32 accumulate (tcgen05, tensor memory), Adam",
         "training_runs": args.surrogate_train, "judge_runs": int(res["runs"] - args.surrogate_train),
         "seconds": {k: round(v, 3) for k, v in res["seconds"].items()}, "seconds_total": total,
+        "note": "this leg's workload (N=1024, 4000 steps per run, the 256 x 256 grid) is not the batched sweep "
+                "leg's (N log-uniform in [1024, 65536], 20,000 steps); both the surrogate and the plain method "
+                "are timed here on this leg's workload",
         "points_per_hour": sur_pph,
         "plain_points_per_hour_at_0.02": plain_pph,
-        "plain_runs_per_point_at_0.02": runs_needed,
+        "plain_timed": {"grid_points": len(subset), "runs_per_point": reps, "runs": len(subset) * reps,
+                        "target": "a point's mean within 0.02 with 95 % probability",
+                        "seconds": plain_s,
+                        "accuracy": {"median_abs_error": float(np.median(plain_err)),
+                                     "q90_abs_error": float(np.quantile(plain_err, 0.9)),
+                                     "frac_within_0.02": float(np.mean(plain_err <= 0.02))}},
+        "plain_points_per_hour_derived": derived_pph,
+        "plain_runs_per_point_at_0.02_standard_error": runs_needed,
         "ratio_vs_plain": sur_pph / plain_pph,
         "accuracy": {"reference": "48 grid points x 256 plain runs", "median_abs_error": float(np.median(err)),
                      "q90_abs_error": float(np.quantile(err, 0.9)), "frac_within_0.02": float(np.mean(err <= 0.02))},
@@ -423,8 +549,8 @@ def run_reference(args, rank, world):
 
 
 def run_legs_only(args, rank, world, local_rank):
-    """Only the sweep and/or surrogate legs (for profiling them alone); the
-    default run measures every leg."""
+    """Only the configuration, cell-list, sweep and/or surrogate legs (for
+    profiling them alone); the default run measures every leg."""
     import torch
 
     from spsslangevinintegration_gb300.replicas import max_over_ranks
@@ -439,6 +565,10 @@ def run_legs_only(args, rank, world, local_rank):
         torch.cuda.synchronize()
 
     line = {"legs": sorted(args.legs)}
+    if "configs" in args.legs:
+        cf = run_config_legs(args, rank, world, barrier, max_over_ranks)
+        if cf is not None:
+            line.update(cf)
     if "cells" in args.legs:
         cl = run_cells_leg(args, rank, world, barrier, max_over_ranks)
         if cl is not None:
@@ -447,6 +577,9 @@ def run_legs_only(args, rank, world, local_rank):
         sw = run_sweep_leg(args, rank, world, barrier, max_over_ranks)
         if sw is not None:
             line["sweep"] = sw
+        sv = run_sweep_leg(args, rank, world, barrier, max_over_ranks, verlet=True)
+        if sv is not None:
+            line["sweep_verlet"] = sv
     if "surrogate" in args.legs and rank == 0:
         line["surrogate"] = run_surrogate_leg(args)
     if rank == 0:
@@ -615,10 +748,17 @@ def run_ours(args, rank, world, local_rank):
         cl = run_cells_leg(args, rank, world, barrier, max_over_ranks)
         if cl is not None:
             line["cells"] = cl
+    if not args.no_configs:
+        cf = run_config_legs(args, rank, world, barrier, max_over_ranks)
+        if cf is not None:
+            line.update(cf)
     if not args.no_sweep:
         sw = run_sweep_leg(args, rank, world, barrier, max_over_ranks)
         if sw is not None:
             line["sweep"] = sw
+        sv = run_sweep_leg(args, rank, world, barrier, max_over_ranks, verlet=True)
+        if sv is not None:
+            line["sweep_verlet"] = sv
     if not args.no_surrogate and rank == 0:
         line["surrogate"] = run_surrogate_leg(args)
     print(json.dumps(line), flush=True)
@@ -640,8 +780,8 @@ def main():
     ap.add_argument("--sweep-steps", type=int, default=400)
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--surrogate-train", type=int, default=50000)
-    ap.add_argument("--legs", default="main,cells,sweep,surrogate",
-                    help="comma-separated subset of main, cells, sweep, surrogate (profiling a leg alone)")
+    ap.add_argument("--legs", default="main,configs,cells,sweep,surrogate",
+                    help="comma-separated subset of main, configs, cells, sweep, surrogate (profiling a leg alone)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -656,6 +796,7 @@ def main():
         dist.init_process_group("nccl")
     args.legs = set(x.strip() for x in args.legs.split(",") if x.strip())
     args.no_cells = "cells" not in args.legs
+    args.no_configs = "configs" not in args.legs
     if "main" in args.legs:
         args.no_sweep = args.no_sweep or "sweep" not in args.legs
         args.no_surrogate = args.no_surrogate or "surrogate" not in args.legs

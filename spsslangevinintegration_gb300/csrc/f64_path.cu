@@ -24,6 +24,7 @@ struct F64Path
   DeviceArray<double> state, rk, k[4], td, det, caf, nat_freq, partials, scratch_state, scratch_kprev,
       scratch_knext;
   DeviceArray<int> cell_of;
+  DeviceArray<float2> posf;  // stage positions wrapped into the box, float (all-pairs range pre-test)
   Binner binner;
   int cells_nc = 0;  // cells per side of the last build (0: none)
   DeviceArray<int> vl_count, vl_off, vl_ent;
@@ -31,6 +32,13 @@ struct F64Path
   int vl_built = 0;
   DeviceArray<unsigned long long> max2;
   unsigned long long *h_max2 = nullptr;  // pinned
+  // one RK4 step captured as a CUDA graph (f64_steps), for the dt and
+  // higher-order flag it was captured with
+  cudaGraph_t rk4_graph = nullptr;
+  cudaGraphExec_t rk4_exec = nullptr;
+  double rk4_dt = 0.0;
+  int rk4_higher_order = -1;
+  unsigned long long rk4_launches = 0;  // kernels in the captured step
 };
 
 struct K64
@@ -38,7 +46,13 @@ struct K64
   int model, flavor, n, s;
   double v0, xi, xi_r, xi_phi, sigma, alpha, rho2, rmax2, ca, sa;
   int higher_order;
+  float rho_excl;  // a pair whose float minimum-image distance bound exceeds this is out of range
 };
+
+// Margin of the all-pairs range pre-test, in box units: covers the float
+// rounding of the wrapped positions and of the bound (a few 1e-8) and the
+// FP64 wrap of positions up to 1e4 boxes away (1e-12), many times over.
+constexpr float kPretestMargin = 2e-5f;
 
 static K64 make_k64(const spss_ctx *ctx)
 {
@@ -59,6 +73,7 @@ static K64 make_k64(const spss_ctx *ctx)
   k.ca = std::cos(p.alpha);  // host libm, as the reference's constructor
   k.sa = std::sin(p.alpha);
   k.higher_order = ctx->higher_order;
+  k.rho_excl = (float) (p.rho + 2.0 * kPretestMargin);
   return k;
 }
 
@@ -221,11 +236,37 @@ __global__ void f64_cell_kernel(K64 k, const double *__restrict__ rk, int nc, in
   cell_of[i] = cell_coord(y, nc) * nc + cell_coord(x, nc);
 }
 
+// Stage positions wrapped into the unit box, as floats, for the all-pairs
+// range pre-test.
+__global__ void f64_posf_kernel(K64 k, const double *__restrict__ rk, float2 *__restrict__ posf)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= k.n) return;
+  const double x = rk[(long) k.s * i], y = rk[(long) k.s * i + 1];
+  posf[i] = make_float2((float) (x - floor(x)), (float) (y - floor(y)));
+}
+
+// A lower bound of the minimum-image distance of two particles from their
+// float wrapped positions (exact minimum image of the wrapped coordinates,
+// less the margin): every periodic image the reference's distance functions
+// may pick is at least this far, so a pair whose bound exceeds rho is out of
+// range for the FP64 test as well.
+__device__ __forceinline__ bool pretest_out(const K64 &k, float2 a, float2 b)
+{
+  float dx = fabsf(b.x - a.x), dy = fabsf(b.y - a.y);
+  dx = fmaxf(fminf(dx, 1.0f - dx) - kPretestMargin, 0.0f);
+  dy = fmaxf(fminf(dy, 1.0f - dy) - kPretestMargin, 0.0f);
+  return dx > k.rho_excl || dy > k.rho_excl || dx * dx + dy * dy > k.rho_excl * k.rho_excl;
+}
+
 // All pairs (ParticleSystemFirstOrder.cpp:162-228, ParticleSystemFirstOrderPtr.cpp:225-316,
 // ParticleSystemSecondOrder.cpp:116-177): one warp per particle, lanes stride
-// over j, partial sums combined by a fixed shuffle tree.
-__global__ void f64_allpairs_kernel(K64 k, const double *__restrict__ rk, double *__restrict__ k_next,
-                                    double *__restrict__ caf)
+// over j, partial sums combined by a fixed shuffle tree.  A float pre-test
+// on the wrapped positions excludes the pairs that are certainly out of
+// range; every other pair is decided by the reference's FP64 expression, so
+// the neighbour sets are the FP64 ones.
+__global__ void f64_allpairs_kernel(K64 k, const double *__restrict__ rk, const float2 *__restrict__ posf,
+                                    double *__restrict__ k_next, double *__restrict__ caf)
 {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -240,10 +281,11 @@ __global__ void f64_allpairs_kernel(K64 k, const double *__restrict__ rk, double
     x_i = wrap1(x_i);
     y_i = wrap1(y_i);
   }
+  const float2 pi = posf[i];
   Sums a{0.0, 0.0, 0.0};
   for (int j = lane; j < k.n; j += 32)
   {
-    if (j == i) continue;
+    if (j == i || pretest_out(k, pi, posf[j])) continue;
     const double *sj = rk + (long) k.s * j;
     if (pair_dr2<false>(k, x_i, y_i, sj[0], sj[1]) <= k.rho2) add_pair(k, a, phi_i, omega_i, sj[ip], sj[ip + 1]);
   }
@@ -579,6 +621,7 @@ int f64_create(spss_ctx *ctx)
   SPSS_TRY(f->caf.reserve(ctx->p.n));
   SPSS_TRY(f->nat_freq.reserve(ctx->p.n));
   SPSS_TRY(f->cell_of.reserve(ctx->p.n));
+  SPSS_TRY(f->posf.reserve(ctx->p.n));
   SPSS_TRY(f->vl_count.reserve(ctx->p.n));
   SPSS_TRY(f->vl_off.reserve(ctx->p.n + 1));
   SPSS_TRY(f->max2.reserve(1));
@@ -607,6 +650,9 @@ void f64_destroy(spss_ctx *ctx)
   f->scratch_kprev.release();
   f->scratch_knext.release();
   f->cell_of.release();
+  f->posf.release();
+  if (f->rk4_exec) cudaGraphExecDestroy(f->rk4_exec);
+  if (f->rk4_graph) cudaGraphDestroy(f->rk4_graph);
   f->binner.release();
   f->vl_count.release();
   f->vl_off.release();
@@ -707,8 +753,10 @@ int f64_evaluate(spss_ctx *ctx, int variant, const double *d_state, const double
   switch (variant)
   {
     case SPSS_VARIANT_ALL_PAIRS:
-      f64_allpairs_kernel<<<blocks_for(32L * k.n, 128), 128, 0, ctx->stream>>>(k, f->rk.ptr, d_knext, f->caf.ptr);
-      ++ctx->launches;
+      f64_posf_kernel<<<blocks_for(k.n, 256), 256, 0, ctx->stream>>>(k, f->rk.ptr, f->posf.ptr);
+      f64_allpairs_kernel<<<blocks_for(32L * k.n, 128), 128, 0, ctx->stream>>>(k, f->rk.ptr, f->posf.ptr, d_knext,
+                                                                                f->caf.ptr);
+      ctx->launches += 2;
       return check_launch("f64_allpairs_kernel");
     case SPSS_VARIANT_LINKED_LIST:
       SPSS_TRY(build_cells(ctx, k, ctx->nc));
@@ -829,6 +877,65 @@ int f64_step(spss_ctx *ctx, int stepper, double t, double dt)
     SPSS_TRY(f64_max_displacement(ctx, f->td.ptr, &max2));
     SPSS_TRY(host_calculate_max_displacement(ctx, max2));
   }
+  return SPSS_OK;
+}
+
+// nsteps RK4 steps: one step runs as it is (sizing every buffer), the rest
+// replay that step captured as a CUDA graph — RK4 draws no noise and, without
+// a Verlet list, needs no host decision between steps.  The state is
+// identical to nsteps single steps.  Other steppers and Verlet contexts step
+// one by one.
+int f64_steps(spss_ctx *ctx, int stepper, double t0, double dt, int nsteps)
+{
+  F64Path *f = ctx->f64;
+  double t = t0;
+  const bool graphable = stepper == SPSS_STEPPER_RK4 && !ctx->uses_verlet_list &&
+                         variant_for(ctx, ctx->p.variant) != SPSS_VARIANT_VERLET &&
+                         variant_for(ctx, ctx->p.variant) != SPSS_VARIANT_LINKED_LIST_VERLET;
+  if (!graphable || nsteps < 3)
+  {
+    for (int k = 0; k < nsteps; ++k)
+    {
+      t += dt;
+      SPSS_TRY(f64_step(ctx, stepper, t, dt));
+    }
+    return SPSS_OK;
+  }
+  t += dt;
+  SPSS_TRY(f64_step(ctx, stepper, t, dt));
+  if (!f->rk4_exec || f->rk4_dt != dt || f->rk4_higher_order != ctx->higher_order)
+  {
+    if (f->rk4_exec) cudaGraphExecDestroy(f->rk4_exec);
+    if (f->rk4_graph) cudaGraphDestroy(f->rk4_graph);
+    f->rk4_exec = nullptr;
+    f->rk4_graph = nullptr;
+    cudaStream_t work = ctx->stream;
+    ctx->stream = ctx->own_stream;  // capture needs a non-legacy stream
+    const unsigned long long launches0 = ctx->launches;
+    SPSS_CUDA_TRY(cudaStreamSynchronize(work));
+    int rc = SPSS_OK;
+    if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = SPSS_ERR_CUDA;
+    if (rc == SPSS_OK) rc = f64_step(ctx, stepper, t + dt, dt);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    ctx->stream = work;
+    f->rk4_launches = ctx->launches - launches0;
+    ctx->launches = launches0;
+    if (rc == SPSS_OK && e != cudaSuccess) rc = SPSS_ERR_CUDA;
+    if (rc == SPSS_OK && cudaGraphInstantiate(&f->rk4_exec, g, 0) != cudaSuccess) rc = SPSS_ERR_CUDA;
+    if (rc != SPSS_OK)
+    {
+      cudaGetLastError();
+      if (g) cudaGraphDestroy(g);
+      f->rk4_exec = nullptr;
+      return rc;
+    }
+    f->rk4_graph = g;
+    f->rk4_dt = dt;
+    f->rk4_higher_order = ctx->higher_order;
+  }
+  for (int k = 1; k < nsteps; ++k) SPSS_CUDA_TRY(cudaGraphLaunch(f->rk4_exec, ctx->stream));
+  ctx->launches += f->rk4_launches * (unsigned long long) (nsteps - 1);
   return SPSS_OK;
 }
 

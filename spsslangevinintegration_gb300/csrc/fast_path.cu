@@ -64,7 +64,16 @@ struct SysControl
 {
   double acc;              // accumulated displacement (FP64)
   unsigned int max2_bits;  // max |dr|^2 of the step, FP32 bits (non-negative floats order as ints)
-  int pad;
+  int rebuild;             // this system's lists are rebuilt before the next step (per-system rebuilds)
+};
+
+// FastControl::rebuild: no rebuild, every system, or the systems whose own
+// trigger fired (SysControl::rebuild; batches of Verlet-list systems).
+enum
+{
+  REBUILD_NONE = 0,
+  REBUILD_ALL = 1,
+  REBUILD_FLAGGED = 2
 };
 
 // One independent system of a context (a context holds one or a batch of
@@ -96,7 +105,7 @@ struct FastParams
   int n, nc, cap, model;      // n: slots of the whole context
   int kind, always_rebuild, tile_cells, persistent;
   int nsys, ntiles, first, sub_n;
-  int cell0, sys, pad0, pad1;
+  int cell0, sys, selective, pad1;  // selective: per-system rebuilds (batches of Verlet-list systems)
   float v0, xi, xi_r, xi_phi, sigma, ca, sa;
   float rho2_f, band_f, rmax2_f;
   double rho2_d, half_skin;
@@ -528,10 +537,24 @@ __global__ void fast_download_kernel(double *__restrict__ x, int n, int s, int m
 
 // ---------------------------------------------------------------- rebuild
 
+// Whether this rebuild covers system `sys`: every system, or those whose own
+// trigger fired.  A system left out keeps its slots, cells, tile layouts and
+// lists exactly as its last rebuild made them.
+__device__ __forceinline__ bool rebuilds_system(const FastBuffers &B, int sys)
+{
+  return B.ctrl->rebuild != REBUILD_FLAGGED || B.sysctl[sys].rebuild;
+}
+
 __global__ void fast_cells_kernel(FastParams P, FastBuffers B)
 {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= P.n) return;
+  if (!rebuilds_system(B, B.sys_of[q]))
+  {
+    // sorted by cell since its last rebuild: the stable counting sort leaves it in place
+    B.cell_of[q] = B.cell_sorted[q];
+    return;
+  }
   const int par = B.ctrl->parity;
   const uint4 r = (par ? B.rec1 : B.rec0)[q];
   const uint4 a = (par ? B.aux1 : B.aux0)[q];
@@ -545,6 +568,7 @@ __global__ void fast_permute_kernel(FastParams P, FastBuffers B)
 {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= P.n) return;
+  if (!rebuilds_system(B, B.sys_of[q])) return;  // its order is the identity
   const int par = B.ctrl->parity;
   const int src = B.order[q];
   (par ? B.rec0 : B.rec1)[q] = (par ? B.rec1 : B.rec0)[src];
@@ -556,20 +580,36 @@ __global__ void fast_permute_kernel(FastParams P, FastBuffers B)
   B.cell_sorted[q] = B.cell_of[src];
 }
 
+// A rebuild of every system leaves the permuted records in the other buffer
+// (the parity flips); a rebuild of the flagged systems copies theirs back, so
+// the systems left out keep their records where they are.
 __global__ void fast_copyback_kernel(FastParams P, FastBuffers B)
 {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= P.n) return;
+  if (!rebuilds_system(B, B.sys_of[q])) return;
+  if (B.ctrl->rebuild == REBUILD_FLAGGED)
+  {
+    const int par = B.ctrl->parity;
+    (par ? B.rec1 : B.rec0)[q] = (par ? B.rec0 : B.rec1)[q];
+    (par ? B.aux1 : B.aux0)[q] = (par ? B.aux0 : B.aux1)[q];
+  }
   B.pid[q] = B.pid_tmp[q];
   if (P.model == 2) B.vel[q] = B.vel_tmp[q];
 }
 
-// The permuted state lives in the other buffer; lists are now current.
-__global__ void fast_after_rebuild_kernel(FastControl *ctrl, int permuted)
+// Lists are now current.  One block.
+__global__ void fast_after_rebuild_kernel(FastControl *ctrl, SysControl *sysctl, int nsys, int permuted)
 {
-  if (permuted) ctrl->parity ^= 1;
-  ctrl->rebuild = 0;
-  ctrl->rebuilds += 1;
+  const int mode = ctrl->rebuild;
+  __syncthreads();
+  for (int r = threadIdx.x; r < nsys; r += blockDim.x) sysctl[r].rebuild = 0;
+  if (threadIdx.x == 0)
+  {
+    if (permuted && mode != REBUILD_FLAGGED) ctrl->parity ^= 1;
+    ctrl->rebuild = REBUILD_NONE;
+    ctrl->rebuilds += 1;
+  }
 }
 
 // ---------------------------------------------------------------- tiles
@@ -585,6 +625,10 @@ __global__ void fast_after_rebuild_kernel(FastControl *ctrl, int permuted)
 constexpr int kTileCellsDefault = 32;  // cells per tile unless tuned
 constexpr int kTileCap = 512;     // staged neighbour records per CTA (2 x 8 KiB)
 constexpr int kTileThreads = 128;
+// Resident CTAs per SM the Stochastic Euler tile kernels are compiled for.
+#ifndef SPSS_SE_TILE_BLOCKS
+#define SPSS_SE_TILE_BLOCKS 14
+#endif
 constexpr long long kWaitCycles = 1ll << 31;  // about one second at the SM clock
 
 struct TileLayout
@@ -690,6 +734,7 @@ __global__ void fast_tile_layout_kernel(FastParams P, FastBuffers B)
 {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= P.ntiles) return;
+  if (!rebuilds_system(B, B.tile_sys[t])) return;
   const SysParams *S = B.sys + B.tile_sys[t];
   TileLayout L;
   tile_layout(t - S->tile0, S->nc, P.tile_cells, B.cell_off + S->cell0, L);
@@ -1381,7 +1426,7 @@ __device__ __forceinline__ void init_mbarrier(uint32_t mb)
 // stages no aux words (11 KB) and runs 14 CTAs per SM, which measured faster
 // than 9, 10 or 12 despite a few spilled registers.
 template<int MODEL, int STEPPER, int KIND, bool MULTI>
-__global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9 : 14) fast_tile_kernel(FastParams P, FastBuffers B)
+__global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9 : SPSS_SE_TILE_BLOCKS) fast_tile_kernel(FastParams P, FastBuffers B)
 {
   __shared__ __align__(16) uint4 srec[kTileCap];
   __shared__ __align__(16) uint4 saux[STEPPER == 2 ? kTileCap : 1];  // aux words: SRK only (neighbour omega)
@@ -1568,12 +1613,14 @@ __global__ void __launch_bounds__(kTileThreads) fast_verlet_tile_build_kernel(Fa
   __shared__ unsigned char col_of[kTileCap];
   FastControl *ctrl = B.ctrl;
   const int t = blockIdx.x;
+  if (!rebuilds_system(B, B.tile_sys[t])) return;  // the whole CTA: its tile keeps its lists
   const uint4 *rec = ctrl->parity ? B.rec1 : B.rec0;
   const SysParams *S = B.sys + B.tile_sys[t];
   const uint32_t mb = smem_u32(&mbar);
   if (threadIdx.x == 0)
   {
     tile_max = 0;
+    B.tile_maxcnt[t] = 0;  // the per-slot build below raises it
     L = reinterpret_cast<const TileLayout *>(B.tiles)[t];
     if (L.p_end <= L.p_begin || L.ncols > kRunCells) L.staged = 0;
     if (L.staged)
@@ -1651,11 +1698,13 @@ __global__ void __launch_bounds__(kTileThreads) fast_verlet_tile_build_kernel(Fa
 
 // After a step: advance the noise counter and the buffer parity, accumulate
 // each system's displacement in FP64 and set the rebuild flag
-// (CalculateMaxDisplacement, ParticleSystemFirstOrder.cpp:670-696).  The lists
-// of all systems are rebuilt together, so a rebuild restarts every system's
-// accumulator.  One block.
+// (CalculateMaxDisplacement, ParticleSystemFirstOrder.cpp:670-696).  With
+// per-system rebuilds (`selective`) a system whose trigger fires is flagged
+// and restarts its own accumulator, so each system rebuilds exactly when it
+// would alone; otherwise the lists of all systems are rebuilt together and
+// every accumulator restarts.  One block.
 __global__ void fast_control_kernel(FastControl *ctrl, SysControl *sysctl, const SysParams *sys, int nsys,
-                                    int always_rebuild, int verlet)
+                                    int always_rebuild, int verlet, int selective)
 {
   __shared__ int any;
   if (threadIdx.x == 0) any = 0;
@@ -1666,20 +1715,29 @@ __global__ void fast_control_kernel(FastControl *ctrl, SysControl *sysctl, const
     sysctl[r].max2_bits = 0u;
     if (verlet && !always_rebuild)
     {
-      const double acc = sysctl[r].acc + sqrt(max2);
+      double acc = sysctl[r].acc + sqrt(max2);
+      if (acc > sys[r].half_skin)
+      {
+        any = 1;
+        if (selective)
+        {
+          sysctl[r].rebuild = 1;
+          acc = 0.0;
+        }
+      }
       sysctl[r].acc = acc;
-      if (acc > sys[r].half_skin) any = 1;
     }
   }
   __syncthreads();
-  if (any)
+  if (any && !selective)
     for (int r = threadIdx.x; r < nsys; r += blockDim.x) sysctl[r].acc = 0.0;
   if (threadIdx.x == 0)
   {
     ctrl->step += 1;
     ctrl->parity ^= 1;
     ctrl->tile_next = 0;
-    if (always_rebuild || any) ctrl->rebuild = 1;
+    if (always_rebuild) ctrl->rebuild = REBUILD_ALL;
+    else if (any) ctrl->rebuild = selective ? REBUILD_FLAGGED : REBUILD_ALL;
   }
   __syncthreads();
   if (threadIdx.x == 0) ctrl->acc = sysctl[0].acc;
@@ -2052,6 +2110,7 @@ static FastParams params(spss_ctx *ctx, double dt)
   P.model = p.model;
   P.kind = f->kind;
   P.always_rebuild = f->kind == KIND_CELLS ? 1 : 0;
+  P.selective = f->nsys > 1 && f->kind == KIND_VERLET ? 1 : 0;
   P.tile_cells = f->tile_cells;
   P.persistent = f->persistent;
   P.nsys = f->nsys;
@@ -2351,7 +2410,7 @@ static int launch_rebuild(spss_ctx *ctx, const FastParams &P)
     ++ctx->launches;
     SPSS_TRY(check_launch("fast_copyback_kernel"));
   }
-  fast_after_rebuild_kernel<<<1, 1, 0, ctx->stream>>>(f->ctrl, has_cells(f->kind));
+  fast_after_rebuild_kernel<<<1, 256, 0, ctx->stream>>>(f->ctrl, f->sysctl.ptr, f->nsys, has_cells(f->kind));
   ++ctx->launches;
   SPSS_TRY(check_launch("fast_after_rebuild_kernel"));
   if (has_cells(f->kind))
@@ -2362,7 +2421,6 @@ static int launch_rebuild(spss_ctx *ctx, const FastParams &P)
   }
   if (f->kind == KIND_VERLET)
   {
-    SPSS_CUDA_TRY(cudaMemsetAsync(f->tile_maxcnt.ptr, 0, sizeof(int) * f->tile_maxcnt.count, ctx->stream));
     fast_verlet_tile_build_kernel<<<f->ntiles, kTileThreads, 0, ctx->stream>>>(P, buffers(ctx));
     ++ctx->launches;
     SPSS_TRY(check_launch("fast_verlet_tile_build_kernel"));
@@ -2431,7 +2489,7 @@ static int launch_step(spss_ctx *ctx, int stepper, const FastParams &P)
   if (ctx->timing) SPSS_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
   FastPath *f = ctx->fast;
   fast_control_kernel<<<1, 256, 0, ctx->stream>>>(f->ctrl, f->sysctl.ptr, f->sys.ptr, f->nsys, P.always_rebuild,
-                                                   f->kind == KIND_VERLET || f->trigger_only);
+                                                   f->kind == KIND_VERLET || f->trigger_only, P.selective);
   ++ctx->launches;
   return check_launch("fast_control_kernel");
 }

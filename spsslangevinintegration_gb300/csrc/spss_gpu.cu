@@ -387,7 +387,7 @@ int spss_get_verlet_state(spss_ctx *ctx, double *accumulated_displacement, int *
   if (!ctx) return SPSS_ERR_INVALID_ARGUMENT;
   if (ctx->fast && ctx->stream) SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   if (accumulated_displacement) *accumulated_displacement = ctx->accumulated_displacement;
-  if (should_update_lists) *should_update_lists = ctx->should_update_lists;
+  if (should_update_lists) *should_update_lists = ctx->should_update_lists != 0;
   if (uses_verlet_list) *uses_verlet_list = ctx->uses_verlet_list;
   return SPSS_OK;
 }
@@ -488,13 +488,7 @@ int spss_steps(spss_ctx *ctx, int stepper, double t0, double dt, int nsteps)
   if (!ctx || nsteps < 0) return SPSS_ERR_INVALID_ARGUMENT;
   SPSS_TRY(check_stepper(ctx, stepper));
   if (!is_f64(ctx)) return fast_steps(ctx, stepper, t0, dt, nsteps);
-  double t = t0;
-  for (int k = 0; k < nsteps; ++k)
-  {
-    t += dt;
-    SPSS_TRY(f64_step(ctx, stepper, t, dt));
-  }
-  return SPSS_OK;
+  return f64_steps(ctx, stepper, t0, dt, nsteps);
 }
 
 int spss_step_host(spss_ctx *ctx, int stepper, double *state, long len, double t, double dt)

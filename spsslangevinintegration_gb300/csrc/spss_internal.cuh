@@ -306,6 +306,7 @@ int f64_get_state(spss_ctx *ctx, double *d_aos);
 int f64_evaluate(spss_ctx *ctx, int variant, const double *d_state, const double *d_kprev, double *d_knext,
                  double k_coef, double dt);
 int f64_step(spss_ctx *ctx, int stepper, double t, double dt);
+int f64_steps(spss_ctx *ctx, int stepper, double t0, double dt, int nsteps);
 int f64_noise(spss_ctx *ctx, int stepper, unsigned long long step, double *d_out);
 int f64_max_displacement(spss_ctx *ctx, const double *d_td, double *max2_out);
 int f64_complementary_force(spss_ctx *ctx, double *d_out);

@@ -6,9 +6,9 @@ Checks (exact unless stated):
   * a batch of systems with different sizes and parameters steps every system
     bit for bit as a single-system context with the same parameters does
     (cell lists, rebuilt every step in both), and draws the same noise;
-  * Verlet lists in a batch are rebuilt for all systems when one triggers, so
-    a system's neighbour summation order can differ from its single-context
-    run: 99.9 % of components within 1e-4 relative after 20 steps, median 1e-6;
+  * Verlet lists in a batch are rebuilt per system, when that system's own
+    trigger fires: every system steps bit for bit as alone, through rebuilds
+    on different steps;
   * results do not depend on the tiling (cells per tile, persistent launch);
   * spss_autotune leaves the state as it found it: the tuned run equals an
     untuned one bit for bit;
@@ -97,20 +97,39 @@ def test_batch_noise_is_each_systems_noise():
                 assert np.array_equal(z[per * b.first[r]: per * b.first[r + 1]], ref)
 
 
-def test_batch_verlet_close_to_single_contexts():
+@pytest.mark.parametrize("stepper", [SE, SRK])
+def test_batch_verlet_equals_single_contexts(stepper):
+    """Each system of a Verlet-list batch rebuilds its lists when its own
+    trigger fires, and only then, so it steps bit for bit as it does alone,
+    through rebuilds that fall on different steps for different systems."""
+    from spsslangevinintegration_gb300 import Batch
+
     sl = systems(variant=LINKED_LIST_VERLET, sizes=(4096, 20000, 9000))
     xs = states(sl, seed=20)
-    got = run_batch(sl, xs, SRK, 20)
+    singles = []
     for r, s in enumerate(sl):
-        ref = run_single(s, xs[r], SRK, 20).reshape(-1, 6)
-        g = got[r].reshape(-1, 6)
-        d = g - ref
-        d[:, :2] = min_image(d[:, :2])
-        scale = np.abs(ref).max(axis=0)
-        scale[:2] = 1.0
-        rel = np.abs(d) / (np.abs(ref) + scale)
-        assert np.quantile(rel, 0.999) <= 1e-4, (r, np.quantile(rel, 0.999))
-        assert np.median(rel) <= 1e-6, (r, np.median(rel))
+        from spsslangevinintegration_gb300 import Context
+
+        kw = dict(s)
+        with Context(kw.pop("model"), kw.pop("n"), kw.pop("rho"), **kw) as ctx:
+            ctx.set_state(xs[r])
+            builds = [ctx.rebuild_count]
+            for k in range(20):
+                ctx.steps(stepper, 0.0, DT, 20)
+                builds.append(ctx.rebuild_count)
+            singles.append((ctx.get_state(), builds))
+    with Batch(sl) as b:
+        b.set_state(np.concatenate(xs))
+        b.steps(stepper, 0.0, DT, 400)
+        out = b.get_state()
+        batch_builds = b.rebuild_count
+    for r in range(len(sl)):
+        assert np.array_equal(b.system_rows(out, r), singles[r][0]), "system %d differs from its run alone" % r
+    # every system rebuilt on its own trigger at least once, not all at the same times
+    counts = [sb[1][-1] - sb[1][0] for sb in singles]
+    assert min(counts) >= 2
+    assert [sb[1] for sb in singles].count(singles[0][1]) < len(sl)
+    assert batch_builds > max(counts)
 
 
 @pytest.mark.parametrize("variant,stepper", [(LINKED_LIST, SE), (LINKED_LIST_VERLET, SRK)])

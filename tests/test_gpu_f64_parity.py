@@ -197,3 +197,25 @@ def test_invalid_arguments_are_rejected():
             ctx.set_state(np.zeros(7))
         with pytest.raises(SpssError):
             ctx.step(9, 0.0, 0.01)
+
+
+@pytest.mark.parametrize("variant,rho", [(1, 0.05), (2, 0.05), (5, 0.8), (0, 0.03)])
+def test_rk4_graph_steps_equal_single_steps(variant, rho):
+    """spss_steps replays one captured RK4 step as a CUDA graph on the FP64
+    path (no noise, no host decision between steps): the state equals that of
+    single steps bit for bit, stale torque derivatives included."""
+    from helpers import gpu_context, initial
+
+    p = dict(model=1, n=700, rho=rho, flavor="ptr", v0=0.02, xi=0.1, sigma=1.0, alpha=0.3)
+    x0 = initial(1, 700, 31, omega=0.8)
+    out = []
+    for graph in (False, True):
+        with gpu_context(p, precision=0, variant=variant) as ctx:
+            ctx.set_state(x0)
+            if graph:
+                ctx.steps(0, 0.0, 0.01, 25)
+            else:
+                for k in range(25):
+                    ctx.step(0, (k + 1) * 0.01, 0.01)
+            out.append(ctx.get_state())
+    np.testing.assert_array_equal(out[0], out[1])
