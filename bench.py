@@ -15,15 +15,18 @@ HBM (CUDA events on the library's stream, max over ranks, summed over ranks).
 `e2e`: the same through spss_step_host (host array in, host array out every
 step, the host array page-locked).  `roofline`: the pair-and-update kernel's
 algorithmic bytes over its CUDA-event duration.  `cpu_baseline` (rank 0): the oracle port of the
-reference algorithm on this host's cores.  `cells`: the same workload with
-cell lists rebuilt every step (the reference's linked list) next to the
-oracle port of that cell-list workload.  `sweep`: 512 independent systems
-of the batched parameter sweep stepped as one batch (phase-diagram points
-per hour at 20,000 steps per point).  `surrogate` (rank 0): a 256 x 256
-phase diagram from the learned surrogate with an active-learning round,
-checked against a replica reference, against the plain method's cost at the
-same precision.  `--impl reference` times the oracle port alone on the
-N = 4,194,304 workload.
+reference algorithm on this host's cores.  `config1`, `config2`: the two
+smaller benchmark configurations (first order N = 1000 all pairs RK4 FP64;
+second order N = 65,536 cell list SE) next to the oracle port.  `cells`: the
+same workload with cell lists rebuilt every step (the reference's linked
+list) next to the oracle port of that cell-list workload.  `sweep`: 512
+independent systems of the batched parameter sweep stepped as one batch with
+cell lists (phase-diagram points per hour at 20,000 steps per point);
+`sweep_verlet`: the same with per-system Verlet lists.  `surrogate`
+(rank 0): a 256 x 256 phase diagram from the learned surrogate with an
+active-learning round, checked against a replica reference, against the
+plain method timed at the same precision.  `--impl reference` times the
+oracle port alone on the N = 4,194,304 workload.
 """
 import argparse
 import json
@@ -478,7 +481,8 @@ def run_surrogate_leg(args):
     return {
         "workload": "256 x 256 (sigma in [0, 3], D log in [0.01, 1]) phase diagram of the expected phase and "
                     "velocity order parameters, N=1024, density 2, m=1, v0=0.5, StochasticEuler dt=0.005, 4000 "
-                    "steps per run (time average over the second half, every 10 steps)",
+                    "steps per run (time average over the second half, every 10 steps), linked list + Verlet "
+                    "lists (skin 0.3R) for the surrogate's runs and the plain method's alike",
         "network": "5-128-128-128-4 GELU, BF16 operands, FP32 accumulate (tcgen05, tensor memory), Adam",
         "training_runs": args.surrogate_train, "judge_runs": int(res["runs"] - args.surrogate_train),
         "seconds": {k: round(v, 3) for k, v in res["seconds"].items()}, "seconds_total": total,
@@ -549,8 +553,8 @@ def run_reference(args, rank, world):
 
 
 def run_legs_only(args, rank, world, local_rank):
-    """Only the configuration, cell-list, sweep and/or surrogate legs (for
-    profiling them alone); the default run measures every leg."""
+    """Only the configuration, cell-list, sweep, Verlet-sweep and/or surrogate
+    legs (for profiling them alone); the default run measures every leg."""
     import torch
 
     from spsslangevinintegration_gb300.replicas import max_over_ranks
@@ -577,6 +581,7 @@ def run_legs_only(args, rank, world, local_rank):
         sw = run_sweep_leg(args, rank, world, barrier, max_over_ranks)
         if sw is not None:
             line["sweep"] = sw
+    if "sweep_verlet" in args.legs:
         sv = run_sweep_leg(args, rank, world, barrier, max_over_ranks, verlet=True)
         if sv is not None:
             line["sweep_verlet"] = sv
@@ -756,6 +761,7 @@ def run_ours(args, rank, world, local_rank):
         sw = run_sweep_leg(args, rank, world, barrier, max_over_ranks)
         if sw is not None:
             line["sweep"] = sw
+    if "sweep_verlet" in args.legs:
         sv = run_sweep_leg(args, rank, world, barrier, max_over_ranks, verlet=True)
         if sv is not None:
             line["sweep_verlet"] = sv
@@ -780,8 +786,9 @@ def main():
     ap.add_argument("--sweep-steps", type=int, default=400)
     ap.add_argument("--no-surrogate", action="store_true")
     ap.add_argument("--surrogate-train", type=int, default=50000)
-    ap.add_argument("--legs", default="main,configs,cells,sweep,surrogate",
-                    help="comma-separated subset of main, configs, cells, sweep, surrogate (profiling a leg alone)")
+    ap.add_argument("--legs", default="main,configs,cells,sweep,sweep_verlet,surrogate",
+                    help="comma-separated subset of main, configs, cells, sweep, sweep_verlet, surrogate "
+                         "(profiling a leg alone)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

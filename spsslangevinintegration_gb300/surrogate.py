@@ -115,17 +115,22 @@ def run_values(stats):
 
 
 def simulate(points, steps=2000, sample_every=10, burn_in=None, max_systems=8192, seed=0, first_replica=0,
-             variant=N.LINKED_LIST, autotune=True):
+             variant=N.LINKED_LIST_VERLET, skin=0.3, autotune=True):
     """Plain batched simulation of every point (the judge): spss_batch_stats
     rows, in the order of `points`.  Points go in batches of at most
-    `max_systems` systems, each batch one context stepped as one graph per step."""
+    `max_systems` systems, each batch one context stepped as one graph per
+    step.  By default every system runs the reference's linked list + Verlet
+    routine with skin 0.3 R, its lists rebuilt on its own displacement
+    trigger (the same neighbour sets within R as a cell list, at about half
+    the candidates)."""
     from .sweep import run_sweep
 
     out = []
     for b0 in range(0, len(points), max_systems):
         chunk = points[b0:b0 + max_systems]
         out.append(run_sweep(chunk, steps=steps, sample_every=sample_every, burn_in=burn_in, variant=variant,
-                             seed=seed, autotune=autotune, first_replica=first_replica + b0))
+                             seed=seed, autotune=autotune, first_replica=first_replica + b0,
+                             skin=skin if variant == N.LINKED_LIST_VERLET else 0.0))
     return np.concatenate(out, axis=0) if out else np.zeros((0, N.STATS_PER_SYSTEM))
 
 
