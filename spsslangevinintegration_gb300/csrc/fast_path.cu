@@ -626,8 +626,15 @@ constexpr int kTileCellsDefault = 32;  // cells per tile unless tuned
 constexpr int kTileCap = 512;     // staged neighbour records per CTA (2 x 8 KiB)
 constexpr int kTileThreads = 128;
 // Resident CTAs per SM the Stochastic Euler tile kernels are compiled for.
+// Cell lists: 14 (32 registers, a few spilled; measured faster than 9, 10 or
+// 12).  Verlet lists: 10 (48 registers, 4 to 16 bytes spilled); the 512-system
+// sweep at 36-cell tiles ran 0.684 / 0.623 / 0.553 / 0.573 ms per step at
+// 14 / 12 / 10 / 9.
 #ifndef SPSS_SE_TILE_BLOCKS
 #define SPSS_SE_TILE_BLOCKS 14
+#endif
+#ifndef SPSS_SE_VERLET_TILE_BLOCKS
+#define SPSS_SE_VERLET_TILE_BLOCKS 10
 #endif
 constexpr long long kWaitCycles = 1ll << 31;  // about one second at the SM clock
 
@@ -1423,10 +1430,13 @@ __device__ __forceinline__ void init_mbarrier(uint32_t mb)
 // MULTI: several systems, whose parameters come from the system table (one
 // system: from the kernel's parameter space, which costs no registers).
 // Residency: SRK 9 CTAs per SM (56 registers, 24.7 KB of shared memory); SE
-// stages no aux words (11 KB) and runs 14 CTAs per SM, which measured faster
-// than 9, 10 or 12 despite a few spilled registers.
+// stages no aux words (11 KB) and runs 14 CTAs per SM on cell lists (faster
+// than 9, 10 or 12 despite a few spilled registers) and 10 on Verlet lists.
 template<int MODEL, int STEPPER, int KIND, bool MULTI>
-__global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9 : SPSS_SE_TILE_BLOCKS) fast_tile_kernel(FastParams P, FastBuffers B)
+__global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9
+                                                               : (KIND == KIND_VERLET ? SPSS_SE_VERLET_TILE_BLOCKS
+                                                                                      : SPSS_SE_TILE_BLOCKS))
+    fast_tile_kernel(FastParams P, FastBuffers B)
 {
   __shared__ __align__(16) uint4 srec[kTileCap];
   __shared__ __align__(16) uint4 saux[STEPPER == 2 ? kTileCap : 1];  // aux words: SRK only (neighbour omega)
