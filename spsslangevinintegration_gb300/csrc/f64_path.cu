@@ -236,13 +236,17 @@ __global__ void f64_cell_kernel(K64 k, const double *__restrict__ rk, int nc, in
   cell_of[i] = cell_coord(y, nc) * nc + cell_coord(x, nc);
 }
 
-// Stage positions wrapped into the unit box, as floats, for the all-pairs
-// range pre-test.
-__global__ void f64_posf_kernel(K64 k, const double *__restrict__ rk, float2 *__restrict__ posf)
+// The stage state of one particle per thread (the same expression as
+// f64_stage_kernel, element by element) and its position wrapped into the
+// unit box as floats, for the all-pairs range pre-test.
+__global__ void f64_stage_posf_kernel(K64 k, const double *__restrict__ st, const double *__restrict__ kp,
+                                      double *__restrict__ rk, float2 *__restrict__ posf, double k_coef, double dt)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= k.n) return;
-  const double x = rk[(long) k.s * i], y = rk[(long) k.s * i + 1];
+  const long ii = (long) k.s * i;
+  for (int q = 0; q < k.s; ++q) rk[ii + q] = st[ii + q] + k_coef * dt * kp[ii + q];
+  const double x = rk[ii], y = rk[ii + 1];
   posf[i] = make_float2((float) (x - floor(x)), (float) (y - floor(y)));
 }
 
@@ -283,11 +287,21 @@ __global__ void f64_allpairs_kernel(K64 k, const double *__restrict__ rk, const 
   }
   const float2 pi = posf[i];
   Sums a{0.0, 0.0, 0.0};
-  for (int j = lane; j < k.n; j += 32)
+  // the lane's candidates j = lane, lane + 32, ... in that order; the float
+  // positions of four of them are loaded together
+  for (int j0 = lane; j0 < k.n; j0 += 128)
   {
-    if (j == i || pretest_out(k, pi, posf[j])) continue;
-    const double *sj = rk + (long) k.s * j;
-    if (pair_dr2<false>(k, x_i, y_i, sj[0], sj[1]) <= k.rho2) add_pair(k, a, phi_i, omega_i, sj[ip], sj[ip + 1]);
+    float2 pj[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) pj[u] = j0 + 32 * u < k.n ? posf[j0 + 32 * u] : pi;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+    {
+      const int j = j0 + 32 * u;
+      if (j >= k.n || j == i || pretest_out(k, pi, pj[u])) continue;
+      const double *sj = rk + (long) k.s * j;
+      if (pair_dr2<false>(k, x_i, y_i, sj[0], sj[1]) <= k.rho2) add_pair(k, a, phi_i, omega_i, sj[ip], sj[ip + 1]);
+    }
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1)
@@ -746,17 +760,20 @@ int f64_evaluate(spss_ctx *ctx, int variant, const double *d_state, const double
   const K64 k = make_k64(ctx);
   const long len = (long) k.n * k.s;
   const int tb = 256;
-  f64_stage_kernel<<<blocks_for(len, tb), tb, 0, ctx->stream>>>(d_state, d_kprev, f->rk.ptr, len, k_coef, dt);
+  if (variant == SPSS_VARIANT_ALL_PAIRS)
+    f64_stage_posf_kernel<<<blocks_for(k.n, tb), tb, 0, ctx->stream>>>(k, d_state, d_kprev, f->rk.ptr, f->posf.ptr,
+                                                                       k_coef, dt);
+  else
+    f64_stage_kernel<<<blocks_for(len, tb), tb, 0, ctx->stream>>>(d_state, d_kprev, f->rk.ptr, len, k_coef, dt);
   ++ctx->launches;
   SPSS_TRY(check_launch("f64_stage_kernel"));
   if (k.higher_order) SPSS_CUDA_TRY(cudaMemsetAsync(f->caf.ptr, 0, sizeof(double) * k.n, ctx->stream));
   switch (variant)
   {
     case SPSS_VARIANT_ALL_PAIRS:
-      f64_posf_kernel<<<blocks_for(k.n, 256), 256, 0, ctx->stream>>>(k, f->rk.ptr, f->posf.ptr);
       f64_allpairs_kernel<<<blocks_for(32L * k.n, 128), 128, 0, ctx->stream>>>(k, f->rk.ptr, f->posf.ptr, d_knext,
                                                                                 f->caf.ptr);
-      ctx->launches += 2;
+      ++ctx->launches;
       return check_launch("f64_allpairs_kernel");
     case SPSS_VARIANT_LINKED_LIST:
       SPSS_TRY(build_cells(ctx, k, ctx->nc));

@@ -97,14 +97,14 @@ def test_batch_noise_is_each_systems_noise():
                 assert np.array_equal(z[per * b.first[r]: per * b.first[r + 1]], ref)
 
 
-@pytest.mark.parametrize("stepper", [SE, SRK])
-def test_batch_verlet_equals_single_contexts(stepper):
+@pytest.mark.parametrize("model,stepper", [(2, SE), (2, SRK), (1, SRK)])
+def test_batch_verlet_equals_single_contexts(model, stepper):
     """Each system of a Verlet-list batch rebuilds its lists when its own
     trigger fires, and only then, so it steps bit for bit as it does alone,
     through rebuilds that fall on different steps for different systems."""
     from spsslangevinintegration_gb300 import Batch
 
-    sl = systems(variant=LINKED_LIST_VERLET, sizes=(4096, 20000, 9000))
+    sl = systems(model=model, variant=LINKED_LIST_VERLET, sizes=(4096, 20000, 9000))
     xs = states(sl, seed=20)
     singles = []
     for r, s in enumerate(sl):
