@@ -125,10 +125,10 @@ def test_batch_verlet_equals_single_contexts(model, stepper):
         batch_builds = b.rebuild_count
     for r in range(len(sl)):
         assert np.array_equal(b.system_rows(out, r), singles[r][0]), "system %d differs from its run alone" % r
-    # every system rebuilt on its own trigger at least once, not all at the same times
+    # every system rebuilt on its own trigger at least once, and not all on the
+    # same steps: the batch's rebuild steps (the union) outnumber each system's
     counts = [sb[1][-1] - sb[1][0] for sb in singles]
     assert min(counts) >= 2
-    assert [sb[1] for sb in singles].count(singles[0][1]) < len(sl)
     assert batch_builds > max(counts)
 
 
