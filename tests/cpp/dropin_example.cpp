@@ -7,7 +7,7 @@
 // usage: dropin_example <dir>   reads <dir>/fo_init.bin, <dir>/so_init.bin
 //                                writes fo_final.bin, so_final.bin, so_noise.bin,
 //                                fo_traj.bin, fo_summary.txt, fo_restart.bin,
-//                                {fo,so}_addnoise.bin, {fo,so}_addnoise_z.bin
+//                                {fo,so}_addnoise.bin, {fo,so}_addnoise_z.bin, so_residency.bin
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -97,6 +97,21 @@ int main(int argc, char **argv)
       system.AddNoise(x, derivative, t);
       write_all(dir + "/so_addnoise.bin", derivative);
       write_all(dir + "/so_addnoise_z.bin", z);
+
+      // State residency: the observers read the GPU copy of a stepped array
+      // until the program declares a host change.  All phases set to 0 on the
+      // host: the order parameter is still the GPU copy's, then 1 after
+      // spss::HostStateChanged.
+      std::vector<Real> residency(4);
+      spss::detail::order_parameter(x.data(), n, s, residency[0], residency[1]);
+      for (int i = 0; i < n; ++i) x[(size_t) s * i + 4] = 0.0;
+      spss::detail::order_parameter(x.data(), n, s, residency[2], residency[3]);
+      spss::HostStateChanged(x.data());
+      double host_r = 0.0, host_arg = 1.0;
+      spss::detail::order_parameter(x.data(), n, s, host_r, host_arg);
+      residency.push_back(host_r);
+      residency.push_back(host_arg);
+      write_all(dir + "/so_residency.bin", residency);
     }
     {
       // first-order AddNoise (ParticleSystemFirstOrder.cpp:698-708): sqrt(2 D_phi) N(0,1) into omega only

@@ -35,7 +35,7 @@ def systems(model=2, variant=LINKED_LIST, sizes=(1024, 3000, 8192), seed=5, skin
     for r, n in enumerate(sizes):
         m = (1.0, 0.1, 10.0)[r % 3]
         p = params(model, n, m=m, D=(0.1, 0.01, 1.0)[r % 3], sigma=(1.0, 0.5, 2.5)[r % 3],
-                   v0=(0.5, 1.0, 0.25)[r % 3])
+                   v0=(0.5, 0.83, 0.31)[r % 3])
         kw = {k: p[k] for k in PARAM_KEYS if k in p}
         s = dict(model=model, n=n, rho=p["rho"], precision=F32, variant=variant, seed=seed, replica=r, **kw)
         if variant == LINKED_LIST_VERLET:

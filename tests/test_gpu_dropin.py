@@ -44,6 +44,7 @@ def test_dropin_classes_match_oracle():
         times, frames = read_frames(os.path.join(d, "fo_traj.bin"), 400, 4)
         summary = np.loadtxt(os.path.join(d, "fo_summary.txt"))
         restart = np.fromfile(os.path.join(d, "fo_restart.bin"))
+        residency = np.fromfile(os.path.join(d, "so_residency.bin"))
         addnoise = {m: (np.fromfile(os.path.join(d, m + "_addnoise.bin")),
                         np.fromfile(os.path.join(d, m + "_addnoise_z.bin"))) for m in ("fo", "so")}
 
@@ -89,3 +90,9 @@ def test_dropin_classes_match_oracle():
     np.testing.assert_allclose(d[:, 2], np.sqrt(2.0 * 0.02) * z[:, 0], rtol=1e-15)
     np.testing.assert_allclose(d[:, 3], np.sqrt(2.0 * 0.02) * z[:, 1], rtol=1e-15)
     np.testing.assert_allclose(d[:, 5], np.sqrt(2.0 * 0.1) * z[:, 2], rtol=1e-15)
+
+    # observers read the GPU copy of a stepped array (the same state as the
+    # host array) until spss::HostStateChanged, then the host array
+    r_gpu = ob.order_parameters(2, x)
+    assert abs(residency[0] - r_gpu[0]) <= 1e-12 and abs(residency[2] - r_gpu[0]) <= 1e-12
+    assert residency[4] == 1.0 and residency[5] == 0.0
