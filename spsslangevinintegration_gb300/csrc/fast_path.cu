@@ -48,7 +48,7 @@ struct FastControl
   double acc;               // accumulated displacement of system 0 (FP64)
   int parity;               // current rec/aux buffer
   int rebuild;              // lists (and slot order) rebuilt before the next evaluation
-  unsigned int unused;
+  int cells_fresh;          // cell ids of the current slots were written by the last cell-list step
   int overflow;             // largest Verlet count seen beyond capacity (0: none)
   int rebuilds;             // number of rebuilds performed
   int error;                // bit 0: displacement too large for the fixed-point increment; bit 1: staging
@@ -548,7 +548,7 @@ __device__ __forceinline__ bool rebuilds_system(const FastBuffers &B, int sys)
 __global__ void fast_cells_kernel(FastParams P, FastBuffers B)
 {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= P.n) return;
+  if (q >= P.n || B.ctrl->cells_fresh) return;  // the last step wrote every slot's cell id
   if (!rebuilds_system(B, B.sys_of[q]))
   {
     // sorted by cell since its last rebuild: the stable counting sort leaves it in place
@@ -609,6 +609,7 @@ __global__ void fast_after_rebuild_kernel(FastControl *ctrl, SysControl *sysctl,
     if (permuted && mode != REBUILD_FLAGGED) ctrl->parity ^= 1;
     ctrl->rebuild = REBUILD_NONE;
     ctrl->rebuilds += 1;
+    ctrl->cells_fresh = 0;  // the slots moved
   }
 }
 
@@ -1155,26 +1156,28 @@ __device__ __forceinline__ void sums_forces(const FastParams &P, const Acc &a, f
 template<int MODEL, int STEPPER>
 __device__ __forceinline__ float advance_particle(const FastParams &P, const FastBuffers &B, int q, const uint4 &ri,
                                                   const uint4 &ai, float2 v, float f_w, float C, const float z[6],
-                                                  uint4 *rout, uint4 *aout, int &err);
+                                                  uint4 *rout, uint4 *aout, int &err, int *cell_out = nullptr);
 
 // Derivative from the neighbour sums, SE or SRK update in fixed point, new
 // record.  Returns |dr|^2 of the step.
 template<int MODEL, int STEPPER>
 __device__ __forceinline__ float update_particle(const FastParams &P, const FastBuffers &B, int q, const uint4 &ri,
                                                  const uint4 &ai, float2 v, const Acc &a, const float z[6],
-                                                 uint4 *rout, uint4 *aout, int &err)
+                                                 uint4 *rout, uint4 *aout, int &err, int *cell_out = nullptr)
 {
   float f_w, C;
   sums_forces<STEPPER>(P, a, __uint_as_float(ri.z), __uint_as_float(ri.w), __uint_as_float(ai.w), f_w, C);
-  return advance_particle<MODEL, STEPPER>(P, B, q, ri, ai, v, f_w, C, z, rout, aout, err);
+  return advance_particle<MODEL, STEPPER>(P, B, q, ri, ai, v, f_w, C, z, rout, aout, err, cell_out);
 }
 
 // SE or SRK update in fixed point from the forces, new record.  Returns
-// |dr|^2 of the step.
+// |dr|^2 of the step.  `cell_out` (cell-list steps): the new position's cell
+// id at the slot, which the next step's cell-list rebuild then need not
+// recompute.
 template<int MODEL, int STEPPER>
 __device__ __forceinline__ float advance_particle(const FastParams &P, const FastBuffers &B, int q, const uint4 &ri,
                                                   const uint4 &ai, float2 v, float f_w, float C, const float z[6],
-                                                  uint4 *rout, uint4 *aout, int &err)
+                                                  uint4 *rout, uint4 *aout, int &err, int *cell_out)
 {
   const uint64_t Xi = join64(ri.x, ai.x), Yi = join64(ri.y, ai.y);
   const float cphi = __uint_as_float(ri.z), sphi = __uint_as_float(ri.w);
@@ -1240,6 +1243,7 @@ __device__ __forceinline__ float advance_particle(const FastParams &P, const Fas
   phase_sincos(Pn, sn, cn);
   rout[q] = make_uint4((uint32_t) (Xn >> 32), (uint32_t) (Yn >> 32), __float_as_uint(cn), __float_as_uint(sn));
   aout[q] = make_uint4((uint32_t) Xn, (uint32_t) Yn, Pn, __float_as_uint(__fadd_rn(wi, dw)));
+  if (cell_out) cell_out[q] = P.cell0 + cell_of_fix(Xn, Yn, P.nc);
   // box crossings and phase turns are rare: read-modify-write only then (the
   // counts are kept by original index, so the slot re-sort never moves them)
   if (cx | cy | ct)
@@ -1378,7 +1382,8 @@ __device__ __forceinline__ void step_tile(const FastParams &Q, const FastBuffers
       gather_sums<KIND, STEPPER == 2>(Q, B, rin, ain, q, o.cnt, lp, list_stride, o.r, Xi, Yi, a);
     float z[6];
     draw_noise<MODEL, STEPPER>(Q, B.ctrl->step, o.p, z);
-    d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, o.r, o.a, o.v, a, z, rout, aout, err));
+    d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, o.r, o.a, o.v, a, z, rout, aout, err,
+                                                         KIND == KIND_CELLS ? B.cell_of : nullptr));
   }
 }
 
@@ -1513,7 +1518,8 @@ __global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9
       gather_sums<KIND, STEPPER == 2>(Q, B, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
     float z[6];
     draw_noise<MODEL, STEPPER>(Q, ctrl->step, p, z);
-    d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, ri, ai, v, a, z, rout, aout, err));
+    d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, ri, ai, v, a, z, rout, aout, err,
+                                                         KIND == KIND_CELLS ? B.cell_of : nullptr));
   }
   publish_max(ctrl, B.sysctl, sys, d2max, err);
 }
@@ -1714,7 +1720,7 @@ __global__ void __launch_bounds__(kTileThreads) fast_verlet_tile_build_kernel(Fa
 // would alone; otherwise the lists of all systems are rebuilt together and
 // every accumulator restarts.  One block.
 __global__ void fast_control_kernel(FastControl *ctrl, SysControl *sysctl, const SysParams *sys, int nsys,
-                                    int always_rebuild, int verlet, int selective)
+                                    int always_rebuild, int verlet, int selective, int cells_written)
 {
   __shared__ int any;
   if (threadIdx.x == 0) any = 0;
@@ -1746,6 +1752,7 @@ __global__ void fast_control_kernel(FastControl *ctrl, SysControl *sysctl, const
     ctrl->step += 1;
     ctrl->parity ^= 1;
     ctrl->tile_next = 0;
+    ctrl->cells_fresh = cells_written;
     if (always_rebuild) ctrl->rebuild = REBUILD_ALL;
     else if (any) ctrl->rebuild = selective ? REBUILD_FLAGGED : REBUILD_ALL;
   }
@@ -2499,7 +2506,8 @@ static int launch_step(spss_ctx *ctx, int stepper, const FastParams &P)
   if (ctx->timing) SPSS_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
   FastPath *f = ctx->fast;
   fast_control_kernel<<<1, 256, 0, ctx->stream>>>(f->ctrl, f->sysctl.ptr, f->sys.ptr, f->nsys, P.always_rebuild,
-                                                   f->kind == KIND_VERLET || f->trigger_only, P.selective);
+                                                   f->kind == KIND_VERLET || f->trigger_only, P.selective,
+                                                   f->kind == KIND_CELLS ? 1 : 0);
   ++ctx->launches;
   return check_launch("fast_control_kernel");
 }
@@ -2551,6 +2559,9 @@ int fast_set_state(spss_ctx *ctx, const double *d_aos)
       d_aos, ctx->p.n, ctx->s, ctx->p.model, f->perm_valid ? 1 : 0, buffers(ctx));
   ++ctx->launches;
   SPSS_TRY(check_launch("fast_upload_kernel"));
+  // new positions: the next cell-list rebuild computes the cell ids
+  f->h_ctrl->cells_fresh = 0;
+  SPSS_CUDA_TRY(cudaMemsetAsync(&f->ctrl->cells_fresh, 0, sizeof(int), ctx->stream));
   f->perm_valid = true;
   f->have_state = true;
   return SPSS_OK;
@@ -2844,6 +2855,7 @@ static int restore_snapshot(spss_ctx *ctx)
   SPSS_CUDA_TRY(cudaMemcpyAsync(f->h_ctrl, S.ctrl.ptr, sizeof(FastControl), cudaMemcpyDeviceToHost, st));
   SPSS_CUDA_TRY(cudaStreamSynchronize(st));
   f->h_ctrl->rebuild = 1;
+  f->h_ctrl->cells_fresh = 0;  // cell ids are not part of the snapshot
   SPSS_CUDA_TRY(cudaMemcpyAsync(f->ctrl, f->h_ctrl, sizeof(FastControl), cudaMemcpyHostToDevice, st));
   SPSS_CUDA_TRY(cudaStreamSynchronize(st));
   ctx->step_counter = f->h_ctrl->step;
