@@ -249,8 +249,10 @@ int spss_batch_run(spss_ctx *ctx, int stepper, double t0, double dt, long nsteps
 int spss_batch_stats(spss_ctx *ctx, double *out, long len);
 int spss_batch_reset_stats(spss_ctx *ctx);
 
-/* Tiling of the pair-and-update kernel: cells per tile (one row of a system's
- * cell grid; 1 .. 4096) and launch form (0: one CTA per tile; 1: persistent,
+/* Tiling of the pair-and-update kernel: cells per tile (each row of a
+ * system's cell grid is split into ceil(nc / tile_cells) tiles of whole cells;
+ * with Verlet lists the tiles of a row hold nearly equal numbers of particles,
+ * with cell lists tile_cells cells each; 1 .. 4096) and launch form (0: one CTA per tile; 1: persistent,
  * one wave of CTAs taking tiles from a work counter).  Results do not depend
  * on the tiling; the lists are rebuilt before the next step.  F32 contexts. */
 int spss_set_tiling(spss_ctx *ctx, int tile_cells, int persistent);

@@ -615,13 +615,23 @@ __global__ void fast_after_rebuild_kernel(FastControl *ctrl, SysControl *sysctl,
 
 // ---------------------------------------------------------------- tiles
 //
-// A tile is a run of tile_cells cells of one row of a system's rebuild grid;
-// one CTA steps the particles of a tile.  Slots are sorted by cell, so the tile's
-// particles are one slot range and the records of its 3 x (tile_cells + 2)
-// neighbour cells are at most six slot segments (three rows, each split in
-// two where the periodic x-wrap crosses the row end).  The CTA stages those
-// segments into shared memory with TMA bulk copies; the Verlet list of a
-// particle in a staged tile stores shared-memory indices directly.
+// A tile is a run of whole cells of one row of a system's rebuild grid; one
+// CTA steps the particles of a tile.  A row holds ceil(nc / tile_cells) tiles.
+// With Verlet lists they split the row's particles into runs of nearly equal
+// count (boundaries at cell edges), so a tile of about 120 particles fills
+// its 128 threads whatever the local density, where runs of equal width leave
+// Poisson counts above 128 to a second pass of a few threads (36-cell tiles
+// at N = 4,194,304: 0.1963 -> 0.1882 ms per launch, same bits); the layout is
+// computed once per rebuild.  Cell lists lay their tiles out every step and
+// keep runs of tile_cells cells: the binary searches of the equal-count
+// boundaries, and widths beyond the run table, cost more there than the fuller
+// warps gain (measured 0.622 -> 0.645 ms per step at N = 4,194,304).  Slots are
+// sorted by cell, so the tile's particles are one slot range and the records
+// of its 3 x (width + 2) neighbour cells are at most six slot segments (three
+// rows, each split in two where the periodic x-wrap crosses the row end).
+// The CTA stages those segments into shared memory with TMA bulk copies; the
+// Verlet list of a particle in a staged tile stores shared-memory indices
+// directly.
 
 constexpr int kTileCellsDefault = 32;  // cells per tile unless tuned
 constexpr int kTileCap = 512;     // staged neighbour records per CTA (2 x 8 KiB)
@@ -663,13 +673,43 @@ __host__ __device__ __forceinline__ int tiles_per_row(int nc, int tc)
   return (nc + tc - 1) / tc;
 }
 
+// Equal-count tiles: the row's particles split into `nbx` runs of whole
+// cells, boundary k at the first cell edge where the row's running count
+// reaches k * (row count) / nbx.
+__device__ __forceinline__ int row_target(const int *__restrict__ ro, int nc, int k, int nbx)
+{
+  return ro[0] + (int) ((long long) (ro[nc] - ro[0]) * k / nbx);
+}
+
+__device__ __forceinline__ int first_cell_reaching(const int *__restrict__ ro, int nc, int target)
+{
+  int lo = 0, hi = nc;  // ro[hi] >= target always
+  while (lo < hi)
+  {
+    const int mid = (lo + hi) >> 1;
+    if (ro[mid] >= target) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
+}
+
 // Deterministic layout of tile t of a system (cell offsets `off` of that
 // system's grid; the list build and the step compute the same).
-__device__ void tile_layout(int t, int nc, int tc, const int *__restrict__ off, TileLayout &L)
+__device__ void tile_layout(int t, int nc, int tc, const int *__restrict__ off, bool equal_count, TileLayout &L)
 {
   const int nbx = tiles_per_row(nc, tc);
   const int cy = t / nbx, bx = t - cy * nbx;
-  const int cx_lo = bx * tc, cx_hi = min(nc, cx_lo + tc);
+  const int *ro = off + cy * nc;
+  int cx_lo, cx_hi;
+  if (equal_count)
+  {
+    cx_lo = first_cell_reaching(ro, nc, row_target(ro, nc, bx, nbx));
+    cx_hi = bx + 1 == nbx ? nc : first_cell_reaching(ro, nc, row_target(ro, nc, bx + 1, nbx));
+  } else
+  {
+    cx_lo = bx * tc;
+    cx_hi = min(nc, cx_lo + tc);
+  }
   L.p_begin = off[cy * nc + cx_lo];
   L.p_end = off[cy * nc + cx_hi];
   L.row = cy;
@@ -731,12 +771,6 @@ __device__ void tile_layout(int t, int nc, int tc, const int *__restrict__ off, 
   L.staged = L.total <= kTileCap;
 }
 
-__device__ __forceinline__ int tile_of_cell(int c, int nc, int tc)
-{
-  const int cy = c / nc;
-  return cy * tiles_per_row(nc, tc) + (c - cy * nc) / tc;
-}
-
 // Layout of every tile of every system, once per rebuild.
 __global__ void fast_tile_layout_kernel(FastParams P, FastBuffers B)
 {
@@ -745,7 +779,7 @@ __global__ void fast_tile_layout_kernel(FastParams P, FastBuffers B)
   if (!rebuilds_system(B, B.tile_sys[t])) return;
   const SysParams *S = B.sys + B.tile_sys[t];
   TileLayout L;
-  tile_layout(t - S->tile0, S->nc, P.tile_cells, B.cell_off + S->cell0, L);
+  tile_layout(t - S->tile0, S->nc, P.tile_cells, B.cell_off + S->cell0, P.kind == KIND_VERLET, L);
   reinterpret_cast<TileLayout *>(B.tiles)[t] = L;
 }
 
@@ -847,7 +881,7 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p)
 // the stencil of the rebuild-time cell instead.  This per-slot form (global
 // gathers) serves the tiles whose neighbourhood is not staged; the staged
 // tiles build in fast_verlet_tile_build_kernel.
-__device__ void verlet_build_slot(const FastParams &P, const FastBuffers &B, int q)
+__device__ void verlet_build_slot(const FastParams &P, const FastBuffers &B, int q, int t)
 {
   const int par = B.ctrl->parity;
   const uint4 *rec = par ? B.rec1 : B.rec0;
@@ -858,7 +892,6 @@ __device__ void verlet_build_slot(const FastParams &P, const FastBuffers &B, int
   const int *coff = B.cell_off + S->cell0;
   const int c = B.cell_sorted[q] - S->cell0;
   const int cx = c % nc, cy = c / nc;
-  const int t = S->tile0 + tile_of_cell(c, nc, P.tile_cells);
   const TileLayout L = reinterpret_cast<const TileLayout *>(B.tiles)[t];
   int cnt = 0;
   bool far = false;
@@ -1654,7 +1687,7 @@ __global__ void __launch_bounds__(kTileThreads) fast_verlet_tile_build_kernel(Fa
   if (L.p_end <= L.p_begin) return;
   if (!L.staged)
   {
-    for (int q = L.p_begin + threadIdx.x; q < L.p_end; q += blockDim.x) verlet_build_slot(P, B, q);
+    for (int q = L.p_begin + threadIdx.x; q < L.p_end; q += blockDim.x) verlet_build_slot(P, B, q, t);
     return;
   }
   build_runs(L, B.cell_off + S->cell0, S->nc, runs, col_of, &self_base, &ctrl->error);
