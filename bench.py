@@ -620,7 +620,11 @@ def run_ours(args, rank, world, local_rank):
 
     # tile width and launch form picked by the library's autotuner (trial
     # steps, state restored), then warm-up (graph capture, first list build)
-    tune_ms = None if args.no_autotune else ctx.autotune(SRK, DT, steps=4)
+    if args.tile_cells:
+        ctx.set_tiling(args.tile_cells, False)
+        tune_ms = None
+    else:
+        tune_ms = None if args.no_autotune else ctx.autotune(SRK, DT, steps=4)
     tiling = ctx.tiling()
     t = 0.0
     ctx.steps(SRK, t, DT, args.warmup)
@@ -782,6 +786,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true",
                     help="main leg: keep the default tiling (32 cells per tile, one launch per step)")
+    ap.add_argument("--tile-cells", type=int, default=0,
+                    help="main leg: this tiling (cells per tile, one launch per step) instead of the autotuner's")
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--sweep-steps", type=int, default=400)
     ap.add_argument("--no-surrogate", action="store_true")

@@ -637,8 +637,8 @@ constexpr int kTileCellsDefault = 32;  // cells per tile unless tuned
 constexpr int kTileCap = 512;     // staged neighbour records per CTA (2 x 8 KiB)
 constexpr int kTileThreads = 128;
 // Resident CTAs per SM the Stochastic Euler tile kernels are compiled for.
-// Cell lists: 14 (32 registers, a few spilled; measured faster than 9, 10 or
-// 12).  Verlet lists: 10 (48 registers, 4 to 16 bytes spilled); the 512-system
+// Cell lists: 14 (32 registers, some spilled; the 512-system sweep step ran
+// 1.197 / 1.283 / 1.354 ms at 14 / 12 / 10).  Verlet lists: 10 (48 registers, 4 to 16 bytes spilled); the 512-system
 // sweep at 36-cell tiles ran 0.684 / 0.623 / 0.553 / 0.573 ms per step at
 // 14 / 12 / 10 / 9.
 #ifndef SPSS_SE_TILE_BLOCKS
@@ -1053,7 +1053,11 @@ __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const Fa
 {
   if (KIND == KIND_CELLS && runs)
   {
-    // cell list from the tile's run table: three rows of contiguous staged records
+    // cell list from the tile's run table: three rows of contiguous staged
+    // records.  The guard-band decision is inline for Stochastic Euler (no
+    // call in the loop: the batched 512-system sweep step 1.319 -> 1.197 ms,
+    // N = 65,536 0.0638 -> 0.0622 ms, fewer spills at 32 registers) and out of
+    // line for SRK, whose larger kernel ran 0.7 % slower with it inline.
     const StencilRuns &R = runs[col_of[q - L.p_begin]];
     const int self = q + self_base;
 #pragma unroll 1
@@ -1063,7 +1067,7 @@ __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const Fa
       {
         const int e = R.e[r][u];
         for (int idx = R.s[r][u]; idx < e; ++idx)
-          if (idx != self) candidate_staged<OMEGA, true>(P, ri, Xi, Yi, srec, saux, L, aux, idx, a);
+          if (idx != self) candidate_staged<OMEGA, OMEGA>(P, ri, Xi, Yi, srec, saux, L, aux, idx, a);
       }
     return;
   }
