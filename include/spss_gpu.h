@@ -191,10 +191,11 @@ int spss_get_timing(spss_ctx *ctx, double *kernel_ms, unsigned long long *timed_
 #define SPSS_NOALLOC_MAX_PARTICLES (1L << 30)
 
 /* The order parameters of spss_order_parameters, computed without allocating
- * anything: for callers that must not call cudaMalloc, for instance code that
- * runs while a CUDA graph is being captured (an allocation there breaks the
- * capture) or a real-time loop in which cudaMalloc's implicit device
- * synchronisation would stall.  No counterpart in the reference.
+ * anything: for callers that must not call cudaMalloc, for instance a host
+ * application whose own allocator owns the device memory (a raw cudaMalloc
+ * there can fail, or fragment the pool the application manages) or a
+ * real-time loop in which cudaMalloc's implicit device synchronisation would
+ * stall.  No counterpart in the reference.
  *
  * `state` is a device array of the reference's AoS layout (n*4 or n*6
  * doubles for model 1 or 2), `out4` a device array of 4 doubles that receives

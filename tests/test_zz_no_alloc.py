@@ -1,6 +1,7 @@
 """spss_order_parameters_noalloc: the order-parameter reduction for callers
-that must not allocate device memory (for instance while a CUDA graph is
-being captured), with its scratch in a fixed array inside the library.
+that must not allocate device memory (for instance a host application whose
+own allocator owns the GPU's memory), with its scratch in a fixed array
+inside the library.
 
 Called through the C ABI on device buffers the test owns, twice in a row,
 and compared with the existing entry point spss_order_parameters within the
