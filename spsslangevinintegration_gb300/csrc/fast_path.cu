@@ -1424,9 +1424,9 @@ __device__ __forceinline__ void step_tile(const FastParams &Q, const FastBuffers
   }
 }
 
-// Staging of tile t by thread 0: layout, list geometry, and the bulk copies of
-// the neighbour records, aux words (AUX: SRK, which needs the neighbours'
-// omega) and list rows onto the mbarrier.
+// Staging of tile t by thread 0 (persistent launch): layout, list geometry,
+// and the bulk copies of the neighbour records, aux words (AUX: SRK, which
+// needs the neighbours' omega) and list rows onto the mbarrier.
 template<int KIND, bool AUX>
 __device__ __forceinline__ void stage_tile(const FastParams &P, const FastBuffers &B, int t, const uint4 *rin,
                                            const uint4 *ain, uint4 *srec, uint4 *saux, short *slist, uint32_t mb,
@@ -1459,6 +1459,65 @@ __device__ __forceinline__ void stage_tile(const FastParams &P, const FastBuffer
                      smem_u32(slist)),
                  "l"(B.vl + tile_list_base(P.cap, t, L.p_begin)), "r"(list_bytes), "r"(mb)
                  : "memory");
+}
+
+// Staging of tile t by warp 0 (one launch per step): the layout read one word
+// per lane, then the bulk copies issued by several lanes at once (records:
+// lanes 0..5, aux words: lanes 8..13, list rows: lane 16) after lane 0 has
+// armed the mbarrier with the expected bytes.  Against the same staging by
+// thread 0 alone the benchmark kernel ran 0.1889 -> 0.1853 ms (same bits):
+// the serial layout copy and copy issue sat on every CTA's critical path.
+template<int KIND, bool AUX>
+__device__ __forceinline__ void stage_tile_warp(const FastParams &P, const FastBuffers &B, int t, const uint4 *rin,
+                                                const uint4 *ain, uint4 *srec, uint4 *saux, short *slist, uint32_t mb,
+                                                TileLayout &L, int &list_staged, int &list_stride)
+{
+  constexpr int kWords = (int) (sizeof(TileLayout) / sizeof(int));
+  static_assert(kWords <= 32, "one layout word per lane");
+  const int lane = threadIdx.x & 31;
+  const int *src = reinterpret_cast<const int *>(reinterpret_cast<const TileLayout *>(B.tiles) + t);
+  if (lane < kWords) reinterpret_cast<int *>(&L)[lane] = src[lane];
+  const int rows = KIND == KIND_VERLET ? B.tile_maxcnt[t] : 0;
+  __syncwarp();
+  const int p_begin = L.p_begin, p_end = L.p_end, total = L.total, nseg = L.nseg;
+  const bool staged = L.staged && p_end > p_begin;
+  const int stride = tile_list_stride(p_begin, p_end);
+  const uint32_t list_bytes = 2u * (uint32_t) rows * (uint32_t) stride;
+  const bool lstaged = staged && KIND == KIND_VERLET && rows > 0 && rows * stride <= kListCap;
+  __syncwarp();
+  if (lane == 0)
+  {
+    L.staged = staged ? 1 : 0;
+    list_stride = stride;
+    list_staged = lstaged ? 1 : 0;
+    if (staged)
+    {
+      const uint32_t tx = (AUX ? 32u : 16u) * (uint32_t) total + (lstaged ? list_bytes : 0u);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(tx) : "memory");
+    }
+  }
+  if (!staged) return;
+  __syncwarp();
+  if (lane < nseg)
+  {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(&srec[L.base[lane]])),
+                 "l"(rin + L.start[lane]), "r"(16u * L.len[lane]), "r"(mb)
+                 : "memory");
+  } else if (AUX && lane >= 8 && lane < 8 + nseg)
+  {
+    const int k = lane - 8;
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(&saux[L.base[k]])),
+                 "l"(ain + L.start[k]), "r"(16u * L.len[k]), "r"(mb)
+                 : "memory");
+  } else if (lane == 16 && lstaged)
+  {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(slist)),
+                 "l"(B.vl + tile_list_base(P.cap, t, p_begin)), "r"(list_bytes), "r"(mb)
+                 : "memory");
+  }
 }
 
 __device__ __forceinline__ void init_mbarrier(uint32_t mb)
@@ -1496,10 +1555,11 @@ __global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9
   uint4 *aout = par ? B.aux0 : B.aux1;
   const int t = blockIdx.x;
   const uint32_t mb = smem_u32(&mbar);
-  if (threadIdx.x == 0)
+  if (threadIdx.x < 32)
   {
-    init_mbarrier(mb);
-    stage_tile<KIND, STEPPER == 2>(P, B, t, rin, ain, srec, saux, slist, mb, L, list_staged, list_stride, false);
+    if (threadIdx.x == 0) init_mbarrier(mb);
+    __syncwarp();
+    stage_tile_warp<KIND, STEPPER == 2>(P, B, t, rin, ain, srec, saux, slist, mb, L, list_staged, list_stride);
   }
   __syncthreads();
   const bool staged = L.staged;
