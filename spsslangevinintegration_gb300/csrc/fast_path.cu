@@ -1261,7 +1261,7 @@ __device__ __forceinline__ void sums_forces(const FastParams &P, const Acc &a, f
   C = 0.0f;
   if (a.card > 0)
   {
-    const float inv = 1.0f / (float) a.card;
+    const float inv = __frcp_rn((float) a.card);  // the correctly rounded 1 / N_i, as 1.0f / N_i
     const float S = fmaf(cphi, a.ss, -__fmul_rn(sphi, a.sc));  // sum sin(phi_j - phi_i)
     const float K = fmaf(cphi, a.sc, __fmul_rn(sphi, a.ss));   // sum cos(phi_j - phi_i)
     f_w = fmaf(-P.xi_phi, wi, __fmul_rn(__fmul_rn(P.sigma, fmaf(P.ca, S, -__fmul_rn(P.sa, K))), inv));
@@ -1718,6 +1718,9 @@ __global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9
   uint4 *rout = par ? B.rec0 : B.rec1;
   uint4 *aout = par ? B.aux0 : B.aux1;
   const int t = blockIdx.x;
+  // the noise counter, loaded once with the kernel's first loads (its
+  // latency was exposed before every particle's Philox block)
+  const unsigned long long step_now = ctrl->step;
   const uint32_t mb = smem_u32(&mbar);
   if (threadIdx.x < 32)
   {
@@ -1783,7 +1786,7 @@ __global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9
         maxin = max(maxin, nin);
       }
       float z[6];
-      draw_noise<MODEL, STEPPER>(Q, ctrl->step, o.p, z);
+      draw_noise<MODEL, STEPPER>(Q, step_now, o.p, z);
       d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, o.r, o.a, o.v, a, z, rout, aout, err));
     }
     publish_maxin(B, t, maxin);
@@ -1815,7 +1818,7 @@ __global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9
     else
       gather_sums<KIND, STEPPER == 2>(Q, B, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
     float z[6];
-    draw_noise<MODEL, STEPPER>(Q, ctrl->step, p, z);
+    draw_noise<MODEL, STEPPER>(Q, step_now, p, z);
     d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, ri, ai, v, a, z, rout, aout, err,
                                                          KIND == KIND_CELLS ? B.cell_of : nullptr));
   }
