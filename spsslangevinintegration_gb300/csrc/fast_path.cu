@@ -992,31 +992,13 @@ __global__ void fast_request_inner_kernel(SysControl *sysctl, int nsys)
 
 // Neighbour sums of slot q from global memory (per-slot kernel, and tiles
 // that do not fit shared memory): the Verlet list holds slot offsets.
-template<int KIND, bool OMEGA, bool KEEP = false>
+template<int KIND, bool OMEGA>
 __device__ __forceinline__ void gather_sums(const FastParams &P, const FastBuffers &B, const uint4 *__restrict__ rec,
                                             const uint4 *__restrict__ aux, int q, int cnt, const short *lp, int stride,
-                                            const uint4 &ri, uint64_t Xi, uint64_t Yi, Acc &a,
-                                            unsigned long long *keep = nullptr)
+                                            const uint4 &ri, uint64_t Xi, uint64_t Yi, Acc &a)
 {
   if (KIND == KIND_VERLET)
   {
-    if (KEEP && cnt >= 0)
-    {
-      // walking the whole list to build the inner list: entry by entry, bit m
-      // of `keep` set for the entries within the inner radius (tiles whose
-      // neighbourhood is not staged: rare)
-      const long n = stride;
-      for (int m = 0; m < cnt; ++m)
-      {
-        const int j = q + (int) lp[(long) m * n];
-        const uint4 rj = __ldg(&rec[j]);
-        const float dx = (float) (int) (rj.x - ri.x);
-        const float dy = (float) (int) (rj.y - ri.y);
-        if (fmaf(dx, dx, dy * dy) <= P.rin2_f) *keep |= 1ull << m;
-        candidate<OMEGA, KIND == KIND_CELLS>(P, ri, Xi, Yi, rec, aux, j, a);
-      }
-      return;
-    }
     if (cnt >= 0)
     {
       const long n = stride;
@@ -1112,6 +1094,10 @@ __device__ __forceinline__ void candidate_staged(const FastParams &P, const uint
 }
 
 // Neighbour sums of slot q from the tile's staged records.
+// KEEP (a staged Verlet list walked whole to build the inner list): the
+// entries within the inner radius are also written, in list order, to the
+// front of the particle's own column of the staged list (`keep_col`; an
+// entry goes to a row the walk has already read), and counted in `nin`.
 template<int KIND, bool OMEGA, bool KEEP = false>
 __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const FastBuffers &B, const uint4 *srec,
                                                    const uint4 *saux, const TileLayout &L,
@@ -1119,7 +1105,7 @@ __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const Fa
                                                    int cnt, const short *lp, int stride, const uint4 &ri, uint64_t Xi,
                                                    uint64_t Yi, Acc &a, const StencilRuns *runs,
                                                    const unsigned char *col_of, int self_base,
-                                                   unsigned long long *keep = nullptr)
+                                                   short *keep_col = nullptr, int *nin = nullptr)
 {
   if (KIND == KIND_CELLS && runs)
   {
@@ -1176,7 +1162,7 @@ __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const Fa
         // widened by its error bound: never drops a pair within it)
 #pragma unroll
         for (int k = 0; k < 4; ++k)
-          if (d2[k] <= P.rin2_f) *keep |= 1ull << (m + k);
+          if (d2[k] <= P.rin2_f) keep_col[(long) (*nin)++ * n] = (short) i[k];
       }
       if (!band)
       {
@@ -1191,14 +1177,15 @@ __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const Fa
     }
     for (; m < cnt; ++m)
     {
+      const int e = lp[0];
       if (KEEP)
       {
-        const uint4 rj = srec[lp[0]];
+        const uint4 rj = srec[e];
         const float dx = (float) (int) (rj.x - ri.x);
         const float dy = (float) (int) (rj.y - ri.y);
-        if (fmaf(dx, dx, dy * dy) <= P.rin2_f) *keep |= 1ull << m;
+        if (fmaf(dx, dx, dy * dy) <= P.rin2_f) keep_col[(long) (*nin)++ * n] = (short) e;
       }
-      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, L, aux, lp[0], a);
+      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, L, aux, e, a);
       lp += n;
     }
     return;
@@ -1491,16 +1478,44 @@ __device__ __forceinline__ int walk_count(int raw, int mode)
   return raw < 0 ? -1 : (mode == LIST_INNER ? raw >> 16 : raw & 0xffff);
 }
 
-// Inner list of one particle: the entries of its Verlet list (column `src`,
-// row stride `stride`) whose bit is set in `keep`, in list order, written to
-// its inner-list column `dst`; rows are written in order by all lanes of a
-// warp together, so each store is one row segment.  Returns the count.
-__device__ __forceinline__ int write_inner(const short *src, short *__restrict__ dst, int stride,
-                                           unsigned long long keep)
+// Rows 0 .. count-1 of a particle's list column (row stride `stride`) into
+// its inner-list column; the lanes of a warp write the same row together, so
+// each store is one row segment.
+__device__ __forceinline__ void copy_rows(const short *src, short *__restrict__ dst, int stride, int count)
 {
-  int r = 0;
-  for (; keep; keep &= keep - 1, ++r) dst[(long) r * stride] = src[(long) (__ffsll((long long) keep) - 1) * stride];
-  return r;
+  for (int r = 0; r < count; ++r) dst[(long) r * stride] = src[(long) r * stride];
+}
+
+// The step of one particle that walks its whole Verlet list and builds its
+// inner list (LIST_BUILD).  A staged list is compacted in shared memory during
+// the walk and copied out; a list read from global memory (rare: a tile whose
+// neighbourhood or list block does not fit shared memory) becomes its own
+// inner list.  Returns the inner count (the list's count is kept with it).
+template<int KIND, bool OMEGA>
+__device__ __forceinline__ int walk_and_build_inner(const FastParams &Q, const FastBuffers &B, const uint4 *srec,
+                                                    const uint4 *saux, const TileLayout &L, const uint4 *rin,
+                                                    const uint4 *ain, short *slist, const short *glist,
+                                                    short *inner_col, int list_staged, int stride, bool staged,
+                                                    int q, int i, int cnt, const uint4 &ri, uint64_t Xi, uint64_t Yi,
+                                                    const unsigned char *col_of, int self_base, Acc &a)
+{
+  int nin = 0;
+  if (staged && list_staged)
+  {
+    gather_sums_staged<KIND, OMEGA, true>(Q, B, srec, saux, L, rin, ain, q, cnt, slist + i, stride, ri, Xi, Yi, a,
+                                          nullptr, col_of, self_base, slist + i, &nin);
+    copy_rows(slist + i, inner_col, stride, nin);
+  } else
+  {
+    if (staged)
+      gather_sums_staged<KIND, OMEGA>(Q, B, srec, saux, L, rin, ain, q, cnt, glist + i, stride, ri, Xi, Yi, a,
+                                      nullptr, col_of, self_base);
+    else
+      gather_sums<KIND, OMEGA>(Q, B, rin, ain, q, cnt, glist + i, stride, ri, Xi, Yi, a);
+    nin = max(cnt, 0);
+    copy_rows(glist + i, inner_col, stride, nin);
+  }
+  return nin;
 }
 
 // The particles of one tile, one per thread; `o` holds the thread's first
@@ -1527,15 +1542,11 @@ __device__ __forceinline__ void step_tile(const FastParams &Q, const FastBuffers
     const short *lp = KIND == KIND_VERLET ? (list_staged ? slist + i : glist + i) : nullptr;
     if (KIND == KIND_VERLET && mode == LIST_BUILD)
     {
-      unsigned long long keep = 0ull;
-      if (staged)
-        gather_sums_staged<KIND, STEPPER == 2, true>(Q, B, srec, saux, L, rin, ain, q, cnt, lp, list_stride, o.r,
-                                                     Xi, Yi, a, nullptr, col_of, self_base, &keep);
-      else
-        gather_sums<KIND, STEPPER == 2, true>(Q, B, rin, ain, q, cnt, lp, list_stride, o.r, Xi, Yi, a, &keep);
+      const int nin = walk_and_build_inner<KIND, STEPPER == 2>(Q, B, srec, saux, L, rin, ain, const_cast<short *>(slist),
+                                                              glist, B.vl_in + list_base + i, list_staged, list_stride,
+                                                              staged, q, i, cnt, o.r, Xi, Yi, col_of, self_base, a);
       if (cnt >= 0)
       {
-        const int nin = write_inner(lp, B.vl_in + list_base + i, list_stride, keep);
         B.vl_cnt[q] = cnt | (nin << 16);
         maxin = max(maxin, nin);
       }
@@ -1718,9 +1729,10 @@ __global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9
   uint4 *rout = par ? B.rec0 : B.rec1;
   uint4 *aout = par ? B.aux0 : B.aux1;
   const int t = blockIdx.x;
-  // the noise counter, loaded once with the kernel's first loads (its
-  // latency was exposed before every particle's Philox block)
-  const unsigned long long step_now = ctrl->step;
+  // SRK: the noise counter, loaded once with the kernel's first loads (its
+  // latency was exposed before every particle's Philox block); the Stochastic
+  // Euler kernels, compiled for more CTAs per SM, keep the two registers
+  const unsigned long long step_now = STEPPER == 2 ? ctrl->step : 0ull;
   const uint32_t mb = smem_u32(&mbar);
   if (threadIdx.x < 32)
   {
@@ -1772,21 +1784,16 @@ __global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9
       Acc a{0.f, 0.f, 0.f, 0.f, 0};
       const uint64_t Xi = join64(o.r.x, o.a.x), Yi = join64(o.r.y, o.a.y);
       const int i = q - L.p_begin;
-      const short *lp = list_staged ? slist + i : glist + i;
-      unsigned long long keep = 0ull;
-      if (staged)
-        gather_sums_staged<KIND, STEPPER == 2, true>(Q, B, srec, saux, L, rin, ain, q, cnt, lp, list_stride, o.r, Xi,
-                                                     Yi, a, nullptr, col_of, self_base, &keep);
-      else
-        gather_sums<KIND, STEPPER == 2, true>(Q, B, rin, ain, q, cnt, lp, list_stride, o.r, Xi, Yi, a, &keep);
+      const int nin = walk_and_build_inner<KIND, STEPPER == 2>(
+          Q, B, srec, saux, L, rin, ain, slist, glist, B.vl_in + tile_list_base(P.cap, t, L.p_begin) + i, list_staged,
+          list_stride, staged, q, i, cnt, o.r, Xi, Yi, col_of, self_base, a);
       if (cnt >= 0)
       {
-        const int nin = write_inner(lp, B.vl_in + tile_list_base(P.cap, t, L.p_begin) + i, list_stride, keep);
         B.vl_cnt[q] = cnt | (nin << 16);
         maxin = max(maxin, nin);
       }
       float z[6];
-      draw_noise<MODEL, STEPPER>(Q, step_now, o.p, z);
+      draw_noise<MODEL, STEPPER>(Q, STEPPER == 2 ? step_now : ctrl->step, o.p, z);
       d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, o.r, o.a, o.v, a, z, rout, aout, err));
     }
     publish_maxin(B, t, maxin);
@@ -1818,7 +1825,7 @@ __global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9
     else
       gather_sums<KIND, STEPPER == 2>(Q, B, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
     float z[6];
-    draw_noise<MODEL, STEPPER>(Q, step_now, p, z);
+    draw_noise<MODEL, STEPPER>(Q, STEPPER == 2 ? step_now : ctrl->step, p, z);
     d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, ri, ai, v, a, z, rout, aout, err,
                                                          KIND == KIND_CELLS ? B.cell_of : nullptr));
   }
