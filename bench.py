@@ -611,8 +611,6 @@ def run_ours(args, rank, world, local_rank):
                   r_max=p["r_max"], nc_verlet=p["nc_verlet"], seed=12345, replica=rank)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
-    if args.no_inner_lists:
-        ctx.set_inner_lists(False)
     ctx.set_state(x0)
 
     def barrier():
@@ -717,7 +715,6 @@ def run_ours(args, rank, world, local_rank):
     e2e_value = world * n * e2e_steps / e2e_s
     pinned.free()
     acc, flag, uses = ctx.verlet_state()
-    inner_lists = ctx.inner_lists()
     ctx.close()
 
     if rank != 0:
@@ -740,8 +737,7 @@ def run_ours(args, rank, world, local_rank):
                    "n": n, "l2": "inputs larger than L2 (state %.0f MB + lists %.0f MB)" % (
                        n * 56 / 1e6, n * 4 * (mean_list_length(p) + 1) / 1e6),
                    "parallelism": "replicas x%d" % world,
-                   "tiling": {"tile_cells": tiling[0], "persistent": tiling[1], "autotuned_ms_per_step": tune_ms},
-                   "inner_lists": inner_lists},
+                   "tiling": {"tile_cells": tiling[0], "persistent": tiling[1], "autotuned_ms_per_step": tune_ms}},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "kernel": "fast_tile_kernel<2,2,2> (pair sums + SRK update)",
                      "kernel_ms": avg_kernel_s * 1e3,
@@ -792,8 +788,6 @@ def main():
                     help="main leg: keep the default tiling (32 cells per tile, one launch per step)")
     ap.add_argument("--tile-cells", type=int, default=0,
                     help="main leg: this tiling (cells per tile, one launch per step) instead of the autotuner's")
-    ap.add_argument("--no-inner-lists", action="store_true",
-                    help="main leg: every step walks the whole Verlet lists (same results, for comparison)")
     ap.add_argument("--no-sweep", action="store_true")
     ap.add_argument("--sweep-steps", type=int, default=400)
     ap.add_argument("--no-surrogate", action="store_true")

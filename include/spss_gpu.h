@@ -258,17 +258,6 @@ int spss_batch_reset_stats(spss_ctx *ctx);
  * on the tiling; the lists are rebuilt before the next step.  F32 contexts. */
 int spss_set_tiling(spss_ctx *ctx, int tile_cells, int persistent);
 int spss_get_tiling(spss_ctx *ctx, int *tile_cells, int *persistent);
-/* Inner lists of Verlet-list contexts (F32): the pairs of each particle's
- * Verlet list within rho + a third of the skin, in the list's order, rebuilt
- * from the Verlet list whenever the accumulated largest displacement since
- * their last build passes half that buffer.  Steps in between walk only
- * them; the neighbours within rho and the order of their sums are those of
- * the whole list, so results are bit-identical either way.  On by default
- * where the list capacity is at most 64; get reports whether they are in use.
- * No counterpart in the reference (a refinement of its Verlet list,
- * ParticleSystemFirstOrderPtr.cpp:616-815). */
-int spss_set_inner_lists(spss_ctx *ctx, int enabled);
-int spss_get_inner_lists(spss_ctx *ctx, int *enabled);
 /* Times `steps` steps of every tiling candidate (16 to 64 cells per tile in steps of 4,
  * both launch forms) on the context's current state, keeps the fastest and
  * restores the state, step counter and trigger as they were (the lists are

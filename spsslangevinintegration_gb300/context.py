@@ -281,15 +281,6 @@ class Context:
         N.check(self.L.spss_get_tiling(self.h, ctypes.byref(tc), ctypes.byref(pers)), "spss_get_tiling")
         return tc.value, bool(pers.value)
 
-    # -- inner lists of Verlet-list contexts (F32 contexts; results are bit-identical either way)
-    def set_inner_lists(self, enabled):
-        N.check(self.L.spss_set_inner_lists(self.h, int(bool(enabled))), "spss_set_inner_lists")
-
-    def inner_lists(self):
-        on = ctypes.c_int()
-        N.check(self.L.spss_get_inner_lists(self.h, ctypes.byref(on)), "spss_get_inner_lists")
-        return bool(on.value)
-
     def autotune(self, stepper, dt, steps=5):
         """Fastest tiling over trial steps; the state is restored.  Returns ms per step."""
         ms = ctypes.c_double()

@@ -59,18 +59,12 @@ struct FastControl
   long long sample_from;    // ... and not before this step
 };
 
-// Per-system Verlet trigger state (CalculateMaxDisplacement of each system),
-// and the trigger of the inner lists (pairs within rho + buffer, taken from
-// the Verlet list and rebuilt when the displacement since their last build
-// could bring an excluded pair within rho).
+// Per-system Verlet trigger state (CalculateMaxDisplacement of each system).
 struct SysControl
 {
   double acc;              // accumulated displacement (FP64)
   unsigned int max2_bits;  // max |dr|^2 of the step, FP32 bits (non-negative floats order as ints)
   int rebuild;             // this system's lists are rebuilt before the next step (per-system rebuilds)
-  double acc_in;           // accumulated displacement since the inner lists were built (FP64)
-  int prune;               // the next step walks the whole Verlet lists and rebuilds the inner lists
-  int pad;
 };
 
 // FastControl::rebuild: no rebuild, every system, or the systems whose own
@@ -92,9 +86,7 @@ struct SysParams
   int tile0, ntiles, index, replica;
   float v0, xi, xi_r, xi_phi, sigma, ca, sa, rho2_f;
   float band_f, rmax2_f, b_r, b_phi;
-  float rin2_f, pad_f;     // inner-list radius^2 (FP32 units, widened by the FP32 error bound)
   double rho2_d, half_skin;
-  double half_buffer;      // half of (inner radius - rho): the inner lists' trigger
 };
 
 enum Kind
@@ -113,10 +105,9 @@ struct FastParams
   int n, nc, cap, model;      // n: slots of the whole context
   int kind, always_rebuild, tile_cells, persistent;
   int nsys, ntiles, first, sub_n;
-  int cell0, sys, selective, inner;  // selective: per-system rebuilds (batches of Verlet-list systems);
-                                     // inner: Verlet steps use inner lists (capacity <= 64)
+  int cell0, sys, selective, pad1;  // selective: per-system rebuilds (batches of Verlet-list systems)
   float v0, xi, xi_r, xi_phi, sigma, ca, sa;
-  float rho2_f, band_f, rmax2_f, rin2_f;
+  float rho2_f, band_f, rmax2_f;
   double rho2_d, half_skin;
   float dt, sqdt, half_dt2, half_dt15, inv_sqrt3, b_r, b_phi;
   uint64_t seed;
@@ -135,9 +126,8 @@ struct FastBuffers
   int *cell_of, *cell_sorted;
   const int *cell_off;
   const int *order;
-  short *vl;     // Verlet lists (pairs within r_max), written at rebuild
-  short *vl_in;  // inner lists (the Verlet list's pairs within rho + buffer, same order, same layout)
-  int *vl_cnt;   // Verlet count | inner count << 16 (-1: scan the stencil instead)
+  short *vl;
+  int *vl_cnt;
   float *nu;             // natural frequencies (global field), slot = original index
   double *field;         // Z = <e^{i phi}>, W = <omega e^{i phi}> and derived values (global field)
   double *field_partial; // block partials of the field sums
@@ -146,7 +136,6 @@ struct FastBuffers
   const int *tile_sys;   // system of each tile
   SysControl *sysctl;
   int *tile_maxcnt;  // longest list of each tile (rows to stage)
-  int *tile_maxin;   // longest inner list of each tile
   void *tiles;       // TileLayout of every tile, written at rebuild
   FastControl *ctrl;
 };
@@ -198,8 +187,8 @@ struct FastPath
   DeviceArray<float2> vel, vel_tmp;
   DeviceArray<unsigned> pid, pid_tmp, inv;
   DeviceArray<int2> img;
-  DeviceArray<int> turns, cell_of, cell_sorted, vl_cnt, tile_maxcnt, tile_maxin;
-  DeviceArray<short> vl, vl_in;
+  DeviceArray<int> turns, cell_of, cell_sorted, vl_cnt, tile_maxcnt;
+  DeviceArray<short> vl;
   DeviceArray<unsigned char> tiles;
   DeviceArray<SysParams> sys;
   DeviceArray<int> sys_of, tile_sys;
@@ -212,7 +201,6 @@ struct FastPath
   int ntiles = 0;
   int tile_cells = 32;
   int persistent = 0;
-  bool inner_lists = true;  // Verlet steps walk inner lists where the capacity allows
   int persistent_grid = 0;
   Binner binner;
   FastControl *ctrl = nullptr;    // device
@@ -263,7 +251,6 @@ __device__ __forceinline__ FastParams with_system(const FastParams &P, const Sys
   Q.rho2_f = S.rho2_f;
   Q.band_f = S.band_f;
   Q.rmax2_f = S.rmax2_f;
-  Q.rin2_f = S.rin2_f;
   Q.b_r = S.b_r;
   Q.b_phi = S.b_phi;
   Q.rho2_d = S.rho2_d;
@@ -620,23 +607,13 @@ __global__ void fast_after_permute_kernel(FastControl *ctrl, int permuted)
   ctrl->cells_fresh = 0;  // the slots moved
 }
 
-// Lists are now current: the rebuilt systems' next step walks the new Verlet
-// lists whole and builds their inner lists; the flags are cleared only here,
-// so the layout and list kernels before this one rebuild the flagged systems
-// alone.  One block.
+// Lists are now current.  The flags are cleared only here, after the tile
+// layout and list kernels, so those rebuild the flagged systems alone (with
+// the flags cleared before them, every system's layouts and lists were
+// rebuilt at each flagged rebuild).  One block.
 __global__ void fast_after_rebuild_kernel(FastControl *ctrl, SysControl *sysctl, int nsys)
 {
-  const int mode = ctrl->rebuild;
-  __syncthreads();
-  for (int r = threadIdx.x; r < nsys; r += blockDim.x)
-  {
-    if (mode != REBUILD_FLAGGED || sysctl[r].rebuild)
-    {
-      sysctl[r].prune = 1;
-      sysctl[r].acc_in = 0.0;
-    }
-    sysctl[r].rebuild = 0;
-  }
+  for (int r = threadIdx.x; r < nsys; r += blockDim.x) sysctl[r].rebuild = 0;
   if (threadIdx.x == 0)
   {
     ctrl->rebuild = REBUILD_NONE;
@@ -679,15 +656,6 @@ constexpr int kTileThreads = 128;
 #define SPSS_SE_VERLET_TILE_BLOCKS 10
 #endif
 constexpr long long kWaitCycles = 1ll << 31;  // about one second at the SM clock
-// Inner lists (Verlet-list contexts whose list capacity fits a 64-bit mask of
-// entries): buffer = this part of the skin.  A third of the 0.3 R skin at
-// density 2 walks pi (1.1 R)^2 2 = 7.6 candidates per particle instead of 10.6
-// and rebuilds the inner lists about every tenth step.
-#ifndef SPSS_INNER_FRACTION
-#define SPSS_INNER_FRACTION (1.0 / 3.0)
-#endif
-constexpr double kInnerFraction = SPSS_INNER_FRACTION;
-constexpr int kInnerCapMax = 64;
 
 struct TileLayout
 {
@@ -977,17 +945,6 @@ __device__ void verlet_build_slot(const FastParams &P, const FastBuffers &B, int
   B.vl_cnt[q] = (cnt > P.cap || far) ? -1 : cnt;
 }
 
-// The next step of every system walks its whole Verlet list and builds the
-// inner list (inner lists switched on between steps).  One block.
-__global__ void fast_request_inner_kernel(SysControl *sysctl, int nsys)
-{
-  for (int r = threadIdx.x; r < nsys; r += blockDim.x)
-  {
-    sysctl[r].prune = 1;
-    sysctl[r].acc_in = 0.0;
-  }
-}
-
 // ---------------------------------------------------------------- step
 
 // Neighbour sums of slot q from global memory (per-slot kernel, and tiles
@@ -1094,18 +1051,13 @@ __device__ __forceinline__ void candidate_staged(const FastParams &P, const uint
 }
 
 // Neighbour sums of slot q from the tile's staged records.
-// KEEP (a staged Verlet list walked whole to build the inner list): the
-// entries within the inner radius are also written, in list order, to the
-// front of the particle's own column of the staged list (`keep_col`; an
-// entry goes to a row the walk has already read), and counted in `nin`.
-template<int KIND, bool OMEGA, bool KEEP = false>
+template<int KIND, bool OMEGA>
 __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const FastBuffers &B, const uint4 *srec,
                                                    const uint4 *saux, const TileLayout &L,
                                                    const uint4 *__restrict__ rec, const uint4 *__restrict__ aux, int q,
                                                    int cnt, const short *lp, int stride, const uint4 &ri, uint64_t Xi,
                                                    uint64_t Yi, Acc &a, const StencilRuns *runs,
-                                                   const unsigned char *col_of, int self_base,
-                                                   short *keep_col = nullptr, int *nin = nullptr)
+                                                   const unsigned char *col_of, int self_base)
 {
   if (KIND == KIND_CELLS && runs)
   {
@@ -1156,14 +1108,6 @@ __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const Fa
         d2[k] = fmaf(dx, dx, dy * dy);
         band |= fabsf(d2[k] - P.rho2_f) <= P.band_f;
       }
-      if (KEEP)
-      {
-        // entries within the inner radius (FP32 distance against the radius
-        // widened by its error bound: never drops a pair within it)
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-          if (d2[k] <= P.rin2_f) keep_col[(long) (*nin)++ * n] = (short) i[k];
-      }
       if (!band)
       {
 #pragma unroll
@@ -1177,15 +1121,7 @@ __device__ __forceinline__ void gather_sums_staged(const FastParams &P, const Fa
     }
     for (; m < cnt; ++m)
     {
-      const int e = lp[0];
-      if (KEEP)
-      {
-        const uint4 rj = srec[e];
-        const float dx = (float) (int) (rj.x - ri.x);
-        const float dy = (float) (int) (rj.y - ri.y);
-        if (fmaf(dx, dx, dy * dy) <= P.rin2_f) keep_col[(long) (*nin)++ * n] = (short) e;
-      }
-      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, L, aux, e, a);
+      candidate_staged<OMEGA, false>(P, ri, Xi, Yi, srec, saux, L, aux, lp[0], a);
       lp += n;
     }
     return;
@@ -1248,7 +1184,7 @@ __device__ __forceinline__ void sums_forces(const FastParams &P, const Acc &a, f
   C = 0.0f;
   if (a.card > 0)
   {
-    const float inv = __frcp_rn((float) a.card);  // the correctly rounded 1 / N_i, as 1.0f / N_i
+    const float inv = 1.0f / (float) a.card;
     const float S = fmaf(cphi, a.ss, -__fmul_rn(sphi, a.sc));  // sum sin(phi_j - phi_i)
     const float K = fmaf(cphi, a.sc, __fmul_rn(sphi, a.ss));   // sum cos(phi_j - phi_i)
     f_w = fmaf(-P.xi_phi, wi, __fmul_rn(__fmul_rn(P.sigma, fmaf(P.ca, S, -__fmul_rn(P.sa, K))), inv));
@@ -1460,77 +1396,17 @@ __device__ __forceinline__ OwnParticle load_own(const FastBuffers &B, const uint
   return o;
 }
 
-// Which list a Verlet step walks: the whole Verlet list (LIST_FULL: the
-// context keeps no inner lists), the whole list while building the inner
-// lists (LIST_BUILD: the first step after a rebuild, and whenever the
-// displacement since the inner lists were built reaches half their buffer),
-// or the inner list (LIST_INNER: every pair within rho, in the Verlet list's
-// order, so the sums are the same bits as the whole list's).
-enum
-{
-  LIST_FULL = 0,
-  LIST_BUILD = 1,
-  LIST_INNER = 2
-};
-
-__device__ __forceinline__ int walk_count(int raw, int mode)
-{
-  return raw < 0 ? -1 : (mode == LIST_INNER ? raw >> 16 : raw & 0xffff);
-}
-
-// Rows 0 .. count-1 of a particle's list column (row stride `stride`) into
-// its inner-list column; the lanes of a warp write the same row together, so
-// each store is one row segment.
-__device__ __forceinline__ void copy_rows(const short *src, short *__restrict__ dst, int stride, int count)
-{
-  for (int r = 0; r < count; ++r) dst[(long) r * stride] = src[(long) r * stride];
-}
-
-// The step of one particle that walks its whole Verlet list and builds its
-// inner list (LIST_BUILD).  A staged list is compacted in shared memory during
-// the walk and copied out; a list read from global memory (rare: a tile whose
-// neighbourhood or list block does not fit shared memory) becomes its own
-// inner list.  Returns the inner count (the list's count is kept with it).
-template<int KIND, bool OMEGA>
-__device__ __forceinline__ int walk_and_build_inner(const FastParams &Q, const FastBuffers &B, const uint4 *srec,
-                                                    const uint4 *saux, const TileLayout &L, const uint4 *rin,
-                                                    const uint4 *ain, short *slist, const short *glist,
-                                                    short *inner_col, int list_staged, int stride, bool staged,
-                                                    int q, int i, int cnt, const uint4 &ri, uint64_t Xi, uint64_t Yi,
-                                                    const unsigned char *col_of, int self_base, Acc &a)
-{
-  int nin = 0;
-  if (staged && list_staged)
-  {
-    gather_sums_staged<KIND, OMEGA, true>(Q, B, srec, saux, L, rin, ain, q, cnt, slist + i, stride, ri, Xi, Yi, a,
-                                          nullptr, col_of, self_base, slist + i, &nin);
-    copy_rows(slist + i, inner_col, stride, nin);
-  } else
-  {
-    if (staged)
-      gather_sums_staged<KIND, OMEGA>(Q, B, srec, saux, L, rin, ain, q, cnt, glist + i, stride, ri, Xi, Yi, a,
-                                      nullptr, col_of, self_base);
-    else
-      gather_sums<KIND, OMEGA>(Q, B, rin, ain, q, cnt, glist + i, stride, ri, Xi, Yi, a);
-    nin = max(cnt, 0);
-    copy_rows(glist + i, inner_col, stride, nin);
-  }
-  return nin;
-}
-
 // The particles of one tile, one per thread; `o` holds the thread's first
 // particle, loaded before the wait for the tile's bulk copies.  The noise is
 // drawn after the neighbour walk (fewer registers live across the walk).
-// `maxin`: the longest inner list built (LIST_BUILD).
 template<int MODEL, int STEPPER, int KIND>
 __device__ __forceinline__ void step_tile(const FastParams &Q, const FastBuffers &B, const TileLayout &L,
                                           OwnParticle o, const uint4 *srec, const uint4 *saux, const short *slist,
-                                          long list_base, int list_staged, int list_stride, int mode, bool staged,
+                                          const short *glist, int list_staged, int list_stride, bool staged,
                                           const uint4 *rin, const uint4 *ain, uint4 *rout, uint4 *aout, float &d2max,
-                                          int &err, int &maxin, const StencilRuns *runs, const unsigned char *col_of,
+                                          int &err, const StencilRuns *runs, const unsigned char *col_of,
                                           int self_base)
 {
-  const short *glist = KIND == KIND_VERLET ? (mode == LIST_INNER ? B.vl_in : B.vl) + list_base : nullptr;
   const int q0 = L.p_begin + threadIdx.x;
   for (int q = q0; q < L.p_end; q += blockDim.x)
   {
@@ -1538,32 +1414,17 @@ __device__ __forceinline__ void step_tile(const FastParams &Q, const FastBuffers
     Acc a{0.f, 0.f, 0.f, 0.f, 0};
     const uint64_t Xi = join64(o.r.x, o.a.x), Yi = join64(o.r.y, o.a.y);
     const int i = q - L.p_begin;
-    const int cnt = KIND == KIND_VERLET ? walk_count(o.cnt, mode) : 0;
     const short *lp = KIND == KIND_VERLET ? (list_staged ? slist + i : glist + i) : nullptr;
-    if (KIND == KIND_VERLET && mode == LIST_BUILD)
-    {
-      const int nin = walk_and_build_inner<KIND, STEPPER == 2>(Q, B, srec, saux, L, rin, ain, const_cast<short *>(slist),
-                                                              glist, B.vl_in + list_base + i, list_staged, list_stride,
-                                                              staged, q, i, cnt, o.r, Xi, Yi, col_of, self_base, a);
-      if (cnt >= 0)
-      {
-        B.vl_cnt[q] = cnt | (nin << 16);
-        maxin = max(maxin, nin);
-      }
-    } else if (staged && KIND == KIND_VERLET && list_staged)
-    {
-      // a staged list is walked through its shared-memory pointer, so its
-      // entries are read with shared-memory loads
-      gather_sums_staged<KIND, STEPPER == 2>(Q, B, srec, saux, L, rin, ain, q, cnt, slist + i, list_stride, o.r,
+    // a staged list is walked through its shared-memory pointer, so its
+    // entries are read with shared-memory loads
+    if (staged && KIND == KIND_VERLET && list_staged)
+      gather_sums_staged<KIND, STEPPER == 2>(Q, B, srec, saux, L, rin, ain, q, o.cnt, slist + i, list_stride, o.r,
                                              Xi, Yi, a, nullptr, col_of, self_base);
-    } else if (staged)
-    {
-      gather_sums_staged<KIND, STEPPER == 2>(Q, B, srec, saux, L, rin, ain, q, cnt, lp, list_stride, o.r, Xi, Yi,
+    else if (staged)
+      gather_sums_staged<KIND, STEPPER == 2>(Q, B, srec, saux, L, rin, ain, q, o.cnt, lp, list_stride, o.r, Xi, Yi,
                                              a, runs, col_of, self_base);
-    } else
-    {
-      gather_sums<KIND, STEPPER == 2>(Q, B, rin, ain, q, cnt, lp, list_stride, o.r, Xi, Yi, a);
-    }
+    else
+      gather_sums<KIND, STEPPER == 2>(Q, B, rin, ain, q, o.cnt, lp, list_stride, o.r, Xi, Yi, a);
     float z[6];
     draw_noise<MODEL, STEPPER>(Q, B.ctrl->step, o.p, z);
     d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, o.r, o.a, o.v, a, z, rout, aout, err,
@@ -1571,38 +1432,18 @@ __device__ __forceinline__ void step_tile(const FastParams &Q, const FastBuffers
   }
 }
 
-// The longest inner list of tile t, raised by every warp of its CTA after a
-// LIST_BUILD step (the staging zeroed it; all lanes of the warp call this).
-__device__ __forceinline__ void publish_maxin(const FastBuffers &B, int t, int maxin)
-{
-  maxin = __reduce_max_sync(0xffffffffu, maxin);
-  if ((threadIdx.x & 31) == 0) atomicMax(&B.tile_maxin[t], maxin);
-}
-
-// The list mode of tile t's step (Verlet lists; LIST_FULL otherwise).
-template<int KIND, bool MULTI>
-__device__ __forceinline__ int tile_list_mode(const FastParams &P, const FastBuffers &B, int t)
-{
-  if (KIND != KIND_VERLET || !P.inner) return LIST_FULL;
-  return B.sysctl[MULTI ? B.tile_sys[t] : 0].prune ? LIST_BUILD : LIST_INNER;
-}
-
 // Staging of tile t by thread 0 (persistent launch): layout, list geometry,
 // and the bulk copies of the neighbour records, aux words (AUX: SRK, which
 // needs the neighbours' omega) and list rows onto the mbarrier.
-template<int KIND, bool AUX, bool MULTI>
+template<int KIND, bool AUX>
 __device__ __forceinline__ void stage_tile(const FastParams &P, const FastBuffers &B, int t, const uint4 *rin,
                                            const uint4 *ain, uint4 *srec, uint4 *saux, short *slist, uint32_t mb,
-                                           TileLayout &L, int &list_staged, int &list_stride, int &list_mode,
-                                           bool reuse)
+                                           TileLayout &L, int &list_staged, int &list_stride, bool reuse)
 {
   L = reinterpret_cast<const TileLayout *>(B.tiles)[t];
   if (L.p_end <= L.p_begin) L.staged = 0;
   list_stride = tile_list_stride(L.p_begin, L.p_end);
-  const int mode = tile_list_mode<KIND, MULTI>(P, B, t);
-  list_mode = mode;
-  const int rows = KIND == KIND_VERLET ? (mode == LIST_INNER ? B.tile_maxin[t] : B.tile_maxcnt[t]) : 0;
-  if (mode == LIST_BUILD) B.tile_maxin[t] = 0;  // raised by the CTA's warps after the step
+  const int rows = KIND == KIND_VERLET ? B.tile_maxcnt[t] : 0;
   const uint32_t list_bytes = 2u * (uint32_t) rows * (uint32_t) list_stride;
   list_staged = L.staged && KIND == KIND_VERLET && rows > 0 && rows * list_stride <= kListCap;
   if (!L.staged) return;
@@ -1624,8 +1465,7 @@ __device__ __forceinline__ void stage_tile(const FastParams &P, const FastBuffer
   if (list_staged)
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      smem_u32(slist)),
-                 "l"((mode == LIST_INNER ? B.vl_in : B.vl) + tile_list_base(P.cap, t, L.p_begin)), "r"(list_bytes),
-                 "r"(mb)
+                 "l"(B.vl + tile_list_base(P.cap, t, L.p_begin)), "r"(list_bytes), "r"(mb)
                  : "memory");
 }
 
@@ -1635,21 +1475,17 @@ __device__ __forceinline__ void stage_tile(const FastParams &P, const FastBuffer
 // armed the mbarrier with the expected bytes.  Against the same staging by
 // thread 0 alone the benchmark kernel ran 0.1889 -> 0.1853 ms (same bits):
 // the serial layout copy and copy issue sat on every CTA's critical path.
-template<int KIND, bool AUX, bool MULTI>
+template<int KIND, bool AUX>
 __device__ __forceinline__ void stage_tile_warp(const FastParams &P, const FastBuffers &B, int t, const uint4 *rin,
                                                 const uint4 *ain, uint4 *srec, uint4 *saux, short *slist, uint32_t mb,
-                                                TileLayout &L, int &list_staged, int &list_stride, int &list_mode)
+                                                TileLayout &L, int &list_staged, int &list_stride)
 {
   constexpr int kWords = (int) (sizeof(TileLayout) / sizeof(int));
   static_assert(kWords <= 32, "one layout word per lane");
   const int lane = threadIdx.x & 31;
   const int *src = reinterpret_cast<const int *>(reinterpret_cast<const TileLayout *>(B.tiles) + t);
   if (lane < kWords) reinterpret_cast<int *>(&L)[lane] = src[lane];
-  // both row counts are loaded with the mode, so no load waits on another
-  const int maxcnt = KIND == KIND_VERLET ? B.tile_maxcnt[t] : 0;
-  const int maxin = KIND == KIND_VERLET && P.inner ? B.tile_maxin[t] : 0;
-  const int mode = tile_list_mode<KIND, MULTI>(P, B, t);
-  const int rows = mode == LIST_INNER ? maxin : maxcnt;
+  const int rows = KIND == KIND_VERLET ? B.tile_maxcnt[t] : 0;
   __syncwarp();
   const int p_begin = L.p_begin, p_end = L.p_end, total = L.total, nseg = L.nseg;
   const bool staged = L.staged && p_end > p_begin;
@@ -1662,8 +1498,6 @@ __device__ __forceinline__ void stage_tile_warp(const FastParams &P, const FastB
     L.staged = staged ? 1 : 0;
     list_stride = stride;
     list_staged = lstaged ? 1 : 0;
-    list_mode = mode;
-    if (mode == LIST_BUILD) B.tile_maxin[t] = 0;  // raised by the CTA's warps after the step
     if (staged)
     {
       const uint32_t tx = (AUX ? 32u : 16u) * (uint32_t) total + (lstaged ? list_bytes : 0u);
@@ -1689,8 +1523,7 @@ __device__ __forceinline__ void stage_tile_warp(const FastParams &P, const FastB
   {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      smem_u32(slist)),
-                 "l"((mode == LIST_INNER ? B.vl_in : B.vl) + tile_list_base(P.cap, t, p_begin)), "r"(list_bytes),
-                 "r"(mb)
+                 "l"(B.vl + tile_list_base(P.cap, t, p_begin)), "r"(list_bytes), "r"(mb)
                  : "memory");
   }
 }
@@ -1719,7 +1552,7 @@ __global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9
   __shared__ __align__(16) short slist[KIND == KIND_VERLET ? kListCap : 8];
   __shared__ __align__(8) unsigned long long mbar;
   __shared__ TileLayout L;
-  __shared__ int list_staged, list_stride, list_mode, self_base;
+  __shared__ int list_staged, list_stride, self_base;
   __shared__ StencilRuns runs[KIND == KIND_CELLS ? kRunCells : 1];
   __shared__ unsigned char col_of[KIND == KIND_CELLS ? kTileCap : 4];
   FastControl *ctrl = B.ctrl;
@@ -1729,29 +1562,22 @@ __global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9
   uint4 *rout = par ? B.rec0 : B.rec1;
   uint4 *aout = par ? B.aux0 : B.aux1;
   const int t = blockIdx.x;
-  // SRK: the noise counter, loaded once with the kernel's first loads (its
-  // latency was exposed before every particle's Philox block); the Stochastic
-  // Euler kernels, compiled for more CTAs per SM, keep the two registers
-  const unsigned long long step_now = STEPPER == 2 ? ctrl->step : 0ull;
   const uint32_t mb = smem_u32(&mbar);
   if (threadIdx.x < 32)
   {
     if (threadIdx.x == 0) init_mbarrier(mb);
     __syncwarp();
-    stage_tile_warp<KIND, STEPPER == 2, MULTI>(P, B, t, rin, ain, srec, saux, slist, mb, L, list_staged, list_stride,
-                                               list_mode);
+    stage_tile_warp<KIND, STEPPER == 2>(P, B, t, rin, ain, srec, saux, slist, mb, L, list_staged, list_stride);
   }
   __syncthreads();
   const bool staged = L.staged;
   if (L.p_end <= L.p_begin) return;
-  const int mode = KIND == KIND_VERLET ? list_mode : LIST_FULL;
   const int sys = MULTI ? B.tile_sys[t] : 0;
   const FastParams Q = MULTI ? with_system(P, B.sys[sys]) : P;
   // cell lists: the stencil run table, built while the bulk copies land
   const bool use_runs = KIND == KIND_CELLS && staged && L.ncols <= kRunCells;
   if (use_runs) build_runs(L, B.cell_off + Q.cell0, Q.nc, runs, col_of, &self_base, &ctrl->error);
-  const short *glist =
-      KIND == KIND_VERLET ? (mode == LIST_INNER ? B.vl_in : B.vl) + tile_list_base(P.cap, t, L.p_begin) : nullptr;
+  const short *glist = KIND == KIND_VERLET ? B.vl + tile_list_base(P.cap, t, L.p_begin) : nullptr;
   // the thread's first particle is loaded before the wait for the bulk
   // copies, so its global loads are in flight while the tile lands
   const int q0 = L.p_begin + threadIdx.x;
@@ -1771,35 +1597,6 @@ __global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9
   }
   float d2max = 0.0f;
   int err = 0;
-  if (KIND == KIND_VERLET && mode == LIST_BUILD)
-  {
-    // the whole lists, and the inner lists built from them (after a rebuild,
-    // and about every tenth step): its own loop, so the registers of the
-    // common loop below are those of the inner-list walk alone
-    int maxin = 0;
-    for (int q = q0; q < L.p_end; q += blockDim.x)
-    {
-      if (q != q0) o = load_own<MODEL, KIND>(B, rin, ain, q);
-      const int cnt = walk_count(o.cnt, LIST_BUILD);
-      Acc a{0.f, 0.f, 0.f, 0.f, 0};
-      const uint64_t Xi = join64(o.r.x, o.a.x), Yi = join64(o.r.y, o.a.y);
-      const int i = q - L.p_begin;
-      const int nin = walk_and_build_inner<KIND, STEPPER == 2>(
-          Q, B, srec, saux, L, rin, ain, slist, glist, B.vl_in + tile_list_base(P.cap, t, L.p_begin) + i, list_staged,
-          list_stride, staged, q, i, cnt, o.r, Xi, Yi, col_of, self_base, a);
-      if (cnt >= 0)
-      {
-        B.vl_cnt[q] = cnt | (nin << 16);
-        maxin = max(maxin, nin);
-      }
-      float z[6];
-      draw_noise<MODEL, STEPPER>(Q, STEPPER == 2 ? step_now : ctrl->step, o.p, z);
-      d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, o.r, o.a, o.v, a, z, rout, aout, err));
-    }
-    publish_maxin(B, t, maxin);
-    publish_max(ctrl, B.sysctl, sys, d2max, err);
-    return;
-  }
   // the loop body is step_tile's, written out here: through the shared
   // function this kernel spills and runs 1 % slower
   for (int q = q0; q < L.p_end; q += blockDim.x)
@@ -1808,7 +1605,7 @@ __global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9
     const unsigned p = o.p;
     const uint4 ri = o.r;
     const uint4 ai = o.a;
-    const int cnt = KIND == KIND_VERLET ? walk_count(o.cnt, mode) : 0;
+    const int cnt = o.cnt;
     const float2 v = o.v;
     Acc a{0.f, 0.f, 0.f, 0.f, 0};
     const uint64_t Xi = join64(ri.x, ai.x), Yi = join64(ri.y, ai.y);
@@ -1825,7 +1622,7 @@ __global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9
     else
       gather_sums<KIND, STEPPER == 2>(Q, B, rin, ain, q, cnt, lp, list_stride, ri, Xi, Yi, a);
     float z[6];
-    draw_noise<MODEL, STEPPER>(Q, STEPPER == 2 ? step_now : ctrl->step, p, z);
+    draw_noise<MODEL, STEPPER>(Q, ctrl->step, p, z);
     d2max = fmaxf(d2max, update_particle<MODEL, STEPPER>(Q, B, q, ri, ai, v, a, z, rout, aout, err,
                                                          KIND == KIND_CELLS ? B.cell_of : nullptr));
   }
@@ -1843,7 +1640,7 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_persistent_kernel(F
   __shared__ __align__(16) short slist[KIND == KIND_VERLET ? kListCap : 8];
   __shared__ __align__(8) unsigned long long mbar;
   __shared__ TileLayout L;
-  __shared__ int list_staged, list_stride, list_mode, tile_id, self_base;
+  __shared__ int list_staged, list_stride, tile_id, self_base;
   __shared__ uint32_t phase;  // mbarrier phase of the next staged tile
   __shared__ StencilRuns runs[KIND == KIND_CELLS ? kRunCells : 1];
   __shared__ unsigned char col_of[KIND == KIND_CELLS ? kTileCap : 4];
@@ -1867,8 +1664,8 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_persistent_kernel(F
       const int t = atomicAdd(&ctrl->tile_next, 1);
       tile_id = t;
       if (t < P.ntiles)
-        stage_tile<KIND, STEPPER == 2, MULTI>(P, B, t, rin, ain, srec, saux, slist, mb, L, list_staged,
-                                              list_stride, list_mode, !first);
+        stage_tile<KIND, STEPPER == 2>(P, B, t, rin, ain, srec, saux, slist, mb, L, list_staged, list_stride,
+                                       !first);
     }
     __syncthreads();
     const int t = tile_id;
@@ -1902,19 +1699,16 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_persistent_kernel(F
       if (threadIdx.x == 0) phase = ph ^ 1u;  // read again only after the next barrier
     }
     if (L.p_end <= L.p_begin) continue;
-    const long list_base = KIND == KIND_VERLET ? tile_list_base(P.cap, t, L.p_begin) : 0;
-    const int mode = KIND == KIND_VERLET ? list_mode : LIST_FULL;
+    const short *glist = KIND == KIND_VERLET ? B.vl + tile_list_base(P.cap, t, L.p_begin) : nullptr;
     float d2max = 0.0f;
-    int err = 0, maxin = 0;
+    int err = 0;
     if (!MULTI)
-      step_tile<MODEL, STEPPER, KIND>(P, B, L, o, srec, saux, slist, list_base, list_staged, list_stride, mode,
-                                      staged, rin, ain, rout, aout, d2max, err, maxin, use_runs ? runs : nullptr,
-                                      col_of, self_base);
+      step_tile<MODEL, STEPPER, KIND>(P, B, L, o, srec, saux, slist, glist, list_staged, list_stride, staged, rin,
+                                      ain, rout, aout, d2max, err, use_runs ? runs : nullptr, col_of, self_base);
     else
-      step_tile<MODEL, STEPPER, KIND>(with_system(P, B.sys[sys]), B, L, o, srec, saux, slist, list_base,
-                                      list_staged, list_stride, mode, staged, rin, ain, rout, aout, d2max, err, maxin,
+      step_tile<MODEL, STEPPER, KIND>(with_system(P, B.sys[sys]), B, L, o, srec, saux, slist, glist, list_staged,
+                                      list_stride, staged, rin, ain, rout, aout, d2max, err,
                                       use_runs ? runs : nullptr, col_of, self_base);
-    if (KIND == KIND_VERLET && mode == LIST_BUILD) publish_maxin(B, t, maxin);
     publish_max(ctrl, B.sysctl, sys, d2max, err);
   }
 }
@@ -2031,7 +1825,7 @@ __global__ void __launch_bounds__(kTileThreads) fast_verlet_tile_build_kernel(Fa
 // would alone; otherwise the lists of all systems are rebuilt together and
 // every accumulator restarts.  One block.
 __global__ void fast_control_kernel(FastControl *ctrl, SysControl *sysctl, const SysParams *sys, int nsys,
-                                    int always_rebuild, int verlet, int selective, int cells_written, int inner)
+                                    int always_rebuild, int verlet, int selective, int cells_written)
 {
   __shared__ int any;
   if (threadIdx.x == 0) any = 0;
@@ -2040,17 +1834,6 @@ __global__ void fast_control_kernel(FastControl *ctrl, SysControl *sysctl, const
   {
     const double max2 = (double) __uint_as_float(sysctl[r].max2_bits);
     sysctl[r].max2_bits = 0u;
-    if (inner)
-    {
-      // inner lists: built from the positions this step started from when it
-      // walked the whole lists, so then this step's displacement starts the
-      // sum; due again once an excluded pair (beyond rho + buffer when they
-      // were built) could have come within rho: the sum of the steps' largest
-      // displacements passes half the buffer
-      const double acc_in = (sysctl[r].prune ? 0.0 : sysctl[r].acc_in) + sqrt(max2);
-      sysctl[r].acc_in = acc_in;
-      sysctl[r].prune = acc_in > sys[r].half_buffer ? 1 : 0;
-    }
     if (verlet && !always_rebuild)
     {
       double acc = sysctl[r].acc + sqrt(max2);
@@ -2384,10 +2167,8 @@ static FastBuffers buffers(spss_ctx *ctx)
   B.cell_off = f->binner.offsets.ptr;
   B.order = f->binner.members.ptr;
   B.vl = f->vl.ptr;
-  B.vl_in = f->vl_in.ptr;
   B.vl_cnt = f->vl_cnt.ptr;
   B.tile_maxcnt = f->tile_maxcnt.ptr;
-  B.tile_maxin = f->tile_maxin.ptr;
   B.tiles = f->tiles.ptr;
   B.sys = f->sys.ptr;
   B.sys_of = f->sys_of.ptr;
@@ -2434,13 +2215,6 @@ static SysParams system_params(const spss_params &p, int index, int first, int n
   const double rmax2 = r_max * r_max;
   S.rmax2_f = (float) (area * (rmax2 + 2.0 * (4.0 * r_max * 2.3283064365386963e-10 + 4.0 * rmax2 * 5.9604644775390625e-8)));
   S.half_skin = 0.5 * (r_max - r_min);
-  // inner lists: the Verlet list's pairs within rho + buffer, the buffer a
-  // fixed part of the skin (fewer candidates per step against a walk of the
-  // whole list whenever the displacement reaches half the buffer)
-  const double r_in = r_min + kInnerFraction * (r_max - r_min);
-  const double rin2 = r_in * r_in;
-  S.rin2_f = (float) (area * (rin2 + 2.0 * (4.0 * r_in * 2.3283064365386963e-10 + 4.0 * rin2 * 5.9604644775390625e-8)));
-  S.half_buffer = 0.5 * (r_in - r_min);
   S.b_r = (float) std::sqrt(2.0 * p.D_r);
   S.b_phi = (float) std::sqrt(2.0 * p.D_phi);
   return S;
@@ -2478,8 +2252,6 @@ static FastParams params(spss_ctx *ctx, double dt)
   P.rho2_f = S.rho2_f;
   P.band_f = S.band_f;
   P.rmax2_f = S.rmax2_f;
-  P.rin2_f = S.rin2_f;
-  P.inner = f->inner_lists && f->kind == KIND_VERLET && f->cap <= kInnerCapMax ? 1 : 0;
   P.rho2_d = S.rho2_d;
   P.half_skin = S.half_skin;
   P.b_r = S.b_r;
@@ -2522,9 +2294,7 @@ static int set_tiling(spss_ctx *ctx, int tile_cells)
   if (f->kind == KIND_VERLET)
   {
     SPSS_TRY(f->vl.reserve((size_t) f->cap * ((size_t) ctx->p.n + 16 * (size_t) ntiles + 16)));
-    SPSS_TRY(f->vl_in.reserve((size_t) f->cap * ((size_t) ctx->p.n + 16 * (size_t) ntiles + 16)));
     SPSS_TRY(f->tile_maxcnt.reserve((size_t) ntiles));
-    SPSS_TRY(f->tile_maxin.reserve((size_t) ntiles));
   }
   SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   // lists and layouts follow the tiles: rebuild before the next step
@@ -2721,8 +2491,6 @@ void fast_destroy(spss_ctx *ctx)
   f->vl.release();
   f->vl_cnt.release();
   f->tile_maxcnt.release();
-  f->tile_maxin.release();
-  f->vl_in.release();
   f->tiles.release();
   f->sys.release();
   f->sys_of.release();
@@ -2846,7 +2614,7 @@ static int launch_step(spss_ctx *ctx, int stepper, const FastParams &P)
   FastPath *f = ctx->fast;
   fast_control_kernel<<<1, 256, 0, ctx->stream>>>(f->ctrl, f->sysctl.ptr, f->sys.ptr, f->nsys, P.always_rebuild,
                                                    f->kind == KIND_VERLET || f->trigger_only, P.selective,
-                                                   f->kind == KIND_CELLS ? 1 : 0, P.inner);
+                                                   f->kind == KIND_CELLS ? 1 : 0);
   ++ctx->launches;
   return check_launch("fast_control_kernel");
 }
@@ -3127,35 +2895,6 @@ int fast_set_tiling(spss_ctx *ctx, int tile_cells, int persistent)
   FastPath *f = ctx->fast;
   f->persistent = persistent;
   return set_tiling(ctx, tile_cells);
-}
-
-int fast_set_inner_lists(spss_ctx *ctx, int enabled)
-{
-  FastPath *f = ctx->fast;
-  if (f->inner_lists == (enabled != 0)) return SPSS_OK;
-  f->inner_lists = enabled != 0;
-  if (f->inner_lists)
-  {
-    fast_request_inner_kernel<<<1, 256, 0, ctx->stream>>>(f->sysctl.ptr, f->nsys);
-    ++ctx->launches;
-    SPSS_TRY(check_launch("fast_request_inner_kernel"));
-  }
-  // the step graphs hold the launch parameters
-  for (auto &g : f->graphs)
-  {
-    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
-    if (g.second.graph) cudaGraphDestroy(g.second.graph);
-  }
-  f->graphs.clear();
-  SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
-  return SPSS_OK;
-}
-
-int fast_get_inner_lists(spss_ctx *ctx, int *enabled)
-{
-  FastPath *f = ctx->fast;
-  *enabled = f->inner_lists && f->kind == KIND_VERLET && f->cap <= kInnerCapMax ? 1 : 0;
-  return SPSS_OK;
 }
 
 int fast_get_tiling(spss_ctx *ctx, int *tile_cells, int *persistent)
