@@ -52,9 +52,11 @@ struct FastControl
   int overflow;             // largest Verlet count seen beyond capacity (0: none)
   int rebuilds;             // number of rebuilds performed
   int error;                // bit 0: displacement too large for the fixed-point increment; bit 1: staging
-                            // timeout; bit 2: stencil cell outside the staged segments
+                            // timeout; bit 2: stencil cell outside the staged segments; bit 3: the
+                            // device launch of the rebuild graph was refused
   int uses_verlet;
   int tile_next;            // work counter of the persistent tile kernel
+  int triggered;            // the last step's displacement trigger fired (its rebuild may already be done)
   long long sample_every;   // order-parameter samples after steps that are multiples of this (0: none)
   long long sample_from;    // ... and not before this step
 };
@@ -140,6 +142,20 @@ struct FastBuffers
   FastControl *ctrl;
 };
 
+// How a step graph does the list rebuild: under a conditional node at the
+// start of the step (GRAPH_CONDITIONAL), tail-launched as a device graph by the
+// control kernel when the trigger fires (GRAPH_DEVICE), unconditionally at the
+// start of every step (GRAPH_ALWAYS: cell lists), or not at all (GRAPH_NONE:
+// kinds without lists or trigger).  Rebuilds requested from the host run
+// before the first graph step in the last three forms.
+enum
+{
+  GRAPH_CONDITIONAL = 0,
+  GRAPH_DEVICE = 1,
+  GRAPH_ALWAYS = 2,
+  GRAPH_NONE = 3
+};
+
 // Device copy of the stepping state, for restoring it after trial steps.
 struct Snapshot
 {
@@ -177,8 +193,22 @@ struct GraphEntry
 {
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;
+  // the rebuild as a device-launchable graph, tail-launched by the step's
+  // control kernel when the trigger fires (null: the step graph holds the
+  // rebuild under a conditional node instead)
+  cudaGraphExec_t rebuild_exec = nullptr;
+  cudaGraph_t rebuild_graph = nullptr;
   int per_step = 0;     // kernels of the unconditional part
-  int per_rebuild = 0;  // kernels of the conditional rebuild
+  int per_rebuild = 0;  // kernels of the rebuild
+  int form = 0;         // GRAPH_* below
+  void release()
+  {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (rebuild_exec) cudaGraphExecDestroy(rebuild_exec);
+    if (rebuild_graph) cudaGraphDestroy(rebuild_graph);
+    *this = GraphEntry();
+  }
 };
 
 struct FastPath
@@ -215,6 +245,7 @@ struct FastPath
   bool have_state = false;
   bool perm_valid = false;
   std::map<std::tuple<int, double, int>, GraphEntry> graphs;  // (stepper, dt, with sampling)
+  bool device_rebuild = true;  // rebuilds tail-launched as device graphs (cleared if this device refuses)
   // per-system order parameters and their time averages
   DeviceArray<OrderSums> order_partial;
   DeviceArray<int2> order_items;   // (system, first slot) of every chunk, systems in order
@@ -1824,8 +1855,15 @@ __global__ void __launch_bounds__(kTileThreads) fast_verlet_tile_build_kernel(Fa
 // and restarts its own accumulator, so each system rebuilds exactly when it
 // would alone; otherwise the lists of all systems are rebuilt together and
 // every accumulator restarts.  One block.
+// TAIL (steps run as graphs): `rebuild_exec`, the rebuild as a device graph,
+// is tail-launched here when a rebuild is due, so it runs right after this
+// step's graph and before the next one, and a step without a rebuild needs
+// no conditional node.  A kernel that can launch a graph runs only as a node
+// of a graph, so eager steps use the form without it.
+template<bool TAIL>
 __global__ void fast_control_kernel(FastControl *ctrl, SysControl *sysctl, const SysParams *sys, int nsys,
-                                    int always_rebuild, int verlet, int selective, int cells_written)
+                                    int always_rebuild, int verlet, int selective, int cells_written,
+                                    cudaGraphExec_t rebuild_exec)
 {
   __shared__ int any;
   if (threadIdx.x == 0) any = 0;
@@ -1858,11 +1896,17 @@ __global__ void fast_control_kernel(FastControl *ctrl, SysControl *sysctl, const
     ctrl->parity ^= 1;
     ctrl->tile_next = 0;
     ctrl->cells_fresh = cells_written;
+    ctrl->triggered = (always_rebuild || any) ? 1 : 0;
     if (always_rebuild) ctrl->rebuild = REBUILD_ALL;
     else if (any) ctrl->rebuild = selective ? REBUILD_FLAGGED : REBUILD_ALL;
   }
   __syncthreads();
-  if (threadIdx.x == 0) ctrl->acc = sysctl[0].acc;
+  if (threadIdx.x == 0)
+  {
+    ctrl->acc = sysctl[0].acc;
+    if (TAIL && ctrl->rebuild)
+      if (cudaGraphLaunch(rebuild_exec, cudaStreamGraphTailLaunch) != cudaSuccess) atomicOr(&ctrl->error, 8);
+  }
 }
 
 __global__ void fast_set_condition_kernel(const FastControl *ctrl, cudaGraphConditionalHandle handle)
@@ -2302,11 +2346,7 @@ static int set_tiling(spss_ctx *ctx, int tile_cells)
   ctx->should_update_lists = 1;
   SPSS_CUDA_TRY(cudaMemcpyAsync(&f->ctrl->rebuild, &f->h_ctrl->rebuild, sizeof(int), cudaMemcpyHostToDevice,
                                 ctx->stream));
-  for (auto &g : f->graphs)
-  {
-    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
-    if (g.second.graph) cudaGraphDestroy(g.second.graph);
-  }
+  for (auto &g : f->graphs) g.second.release();
   f->graphs.clear();
   SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return SPSS_OK;
@@ -2469,11 +2509,7 @@ void fast_destroy(spss_ctx *ctx)
 {
   FastPath *f = ctx->fast;
   if (!f) return;
-  for (auto &g : f->graphs)
-  {
-    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
-    if (g.second.graph) cudaGraphDestroy(g.second.graph);
-  }
+  for (auto &g : f->graphs) g.second.release();
   for (int b = 0; b < 2; ++b)
   {
     f->rec[b].release();
@@ -2595,7 +2631,7 @@ static void launch_step_kind(spss_ctx *ctx, const FastParams &P, const FastBuffe
   }
 }
 
-static int launch_step(spss_ctx *ctx, int stepper, const FastParams &P)
+static int launch_step(spss_ctx *ctx, int stepper, const FastParams &P, cudaGraphExec_t rebuild_exec = nullptr)
 {
   const FastBuffers B = buffers(ctx);
   if (ctx->timing) SPSS_CUDA_TRY(cudaEventRecord(ctx->ev0, ctx->stream));
@@ -2612,9 +2648,14 @@ static int launch_step(spss_ctx *ctx, int stepper, const FastParams &P)
   SPSS_TRY(check_launch("fast_step_kernel"));
   if (ctx->timing) SPSS_CUDA_TRY(cudaEventRecord(ctx->ev1, ctx->stream));
   FastPath *f = ctx->fast;
-  fast_control_kernel<<<1, 256, 0, ctx->stream>>>(f->ctrl, f->sysctl.ptr, f->sys.ptr, f->nsys, P.always_rebuild,
-                                                   f->kind == KIND_VERLET || f->trigger_only, P.selective,
-                                                   f->kind == KIND_CELLS ? 1 : 0);
+  if (rebuild_exec)
+    fast_control_kernel<true><<<1, 256, 0, ctx->stream>>>(f->ctrl, f->sysctl.ptr, f->sys.ptr, f->nsys,
+                                                          P.always_rebuild, f->kind == KIND_VERLET || f->trigger_only,
+                                                          P.selective, f->kind == KIND_CELLS ? 1 : 0, rebuild_exec);
+  else
+    fast_control_kernel<false><<<1, 256, 0, ctx->stream>>>(f->ctrl, f->sysctl.ptr, f->sys.ptr, f->nsys,
+                                                           P.always_rebuild, f->kind == KIND_VERLET || f->trigger_only,
+                                                           P.selective, f->kind == KIND_CELLS ? 1 : 0, nullptr);
   ++ctx->launches;
   return check_launch("fast_control_kernel");
 }
@@ -2635,6 +2676,14 @@ static int launch_sampling(spss_ctx *ctx, const FastParams &P, int gated)
   return check_launch("fast_order_finish_kernel");
 }
 
+// The reference's should_update_lists after a step: set by the trigger until
+// the next evaluation rebuilds.  A graph step performs its rebuild at once
+// (tail launch), so the flag reads from the trigger of the last step as well.
+static int reported_list_flag(const FastControl *c)
+{
+  return (c->rebuild || c->triggered) ? 1 : 0;
+}
+
 static int sync_control(spss_ctx *ctx)
 {
   FastPath *f = ctx->fast;
@@ -2642,7 +2691,8 @@ static int sync_control(spss_ctx *ctx)
   SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   ctx->step_counter = f->h_ctrl->step;
   ctx->accumulated_displacement = f->h_ctrl->acc;
-  ctx->should_update_lists = f->h_ctrl->rebuild;
+  ctx->should_update_lists = reported_list_flag(f->h_ctrl);
+  if (f->h_ctrl->error & ~1) return SPSS_ERR_CUDA;  // a bounded wait ran out, or a device launch failed
   if (f->h_ctrl->error) return SPSS_ERR_NONFINITE;
   return SPSS_OK;
 }
@@ -2652,9 +2702,14 @@ static int sync_control(spss_ctx *ctx)
 static int push_host_control(spss_ctx *ctx)
 {
   FastPath *f = ctx->fast;
-  if (f->h_ctrl->step == ctx->step_counter && f->h_ctrl->rebuild == ctx->should_update_lists) return SPSS_OK;
+  if (f->h_ctrl->step == ctx->step_counter && reported_list_flag(f->h_ctrl) == ctx->should_update_lists)
+    return SPSS_OK;
+  if (reported_list_flag(f->h_ctrl) != ctx->should_update_lists)
+  {
+    f->h_ctrl->rebuild = ctx->should_update_lists ? REBUILD_ALL : REBUILD_NONE;
+    f->h_ctrl->triggered = 0;
+  }
   f->h_ctrl->step = ctx->step_counter;
-  f->h_ctrl->rebuild = ctx->should_update_lists;
   SPSS_CUDA_TRY(cudaMemcpyAsync(f->ctrl, f->h_ctrl, sizeof(FastControl), cudaMemcpyHostToDevice, ctx->stream));
   return SPSS_OK;
 }
@@ -2669,6 +2724,15 @@ int fast_set_state(spss_ctx *ctx, const double *d_aos)
   // new positions: the next cell-list rebuild computes the cell ids
   f->h_ctrl->cells_fresh = 0;
   SPSS_CUDA_TRY(cudaMemsetAsync(&f->ctrl->cells_fresh, 0, sizeof(int), ctx->stream));
+  // the last step's trigger fired and a graph step already rebuilt the lists
+  // from the positions before this upload: the reference rebuilds from the
+  // state it is given next, so rebuild again before the next step
+  if (f->h_ctrl->triggered && !f->h_ctrl->rebuild)
+  {
+    f->h_ctrl->rebuild = REBUILD_ALL;
+    SPSS_CUDA_TRY(cudaMemcpyAsync(&f->ctrl->rebuild, &f->h_ctrl->rebuild, sizeof(int), cudaMemcpyHostToDevice,
+                                  ctx->stream));
+  }
   f->perm_valid = true;
   f->have_state = true;
   return SPSS_OK;
@@ -2722,8 +2786,9 @@ static int build_graph(spss_ctx *ctx, int stepper, double dt, int sampling, Grap
   return rc_all;
 }
 
-static int build_graph_on(spss_ctx *ctx, int stepper, const FastParams &P, int sampling, GraphEntry &g,
-                          unsigned long long launches0)
+// The conditional form: set-condition kernel, IF rebuild, step and control.
+static int build_graph_conditional(spss_ctx *ctx, int stepper, const FastParams &P, int sampling, GraphEntry &g,
+                                   unsigned long long launches0)
 {
   FastPath *f = ctx->fast;
   cudaGraph_t graph;
@@ -2769,6 +2834,82 @@ static int build_graph_on(spss_ctx *ctx, int stepper, const FastParams &P, int s
   SPSS_CUDA_TRY(cudaGraphInstantiate(&g.exec, graph, 0));
   g.graph = graph;
   g.per_step = (int) (ctx->launches - launches0) - g.per_rebuild;
+  g.form = GRAPH_CONDITIONAL;
+  ctx->launches = launches0;  // captured, not launched
+  return SPSS_OK;
+}
+
+// The rebuild as a graph that the control kernel can launch on the device.
+static int build_device_rebuild(spss_ctx *ctx, const FastParams &P, GraphEntry &g)
+{
+  cudaGraph_t rg = nullptr;
+  const unsigned long long before = ctx->launches;
+  SPSS_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
+  const int rc = launch_rebuild(ctx, P);
+  const cudaError_t e = cudaStreamEndCapture(ctx->stream, &rg);
+  g.per_rebuild = (int) (ctx->launches - before);
+  if (rc != SPSS_OK)
+  {
+    if (rg) cudaGraphDestroy(rg);
+    return rc;
+  }
+  SPSS_CUDA_TRY(e);
+  g.rebuild_graph = rg;
+  SPSS_CUDA_TRY(cudaGraphInstantiate(&g.rebuild_exec, rg, cudaGraphInstantiateFlagDeviceLaunch));
+  SPSS_CUDA_TRY(cudaGraphUpload(g.rebuild_exec, ctx->stream));
+  SPSS_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return SPSS_OK;
+}
+
+// One step as a graph.  Verlet lists (and the trigger of list-less Verlet
+// contexts): step and control, the control kernel tail-launching the rebuild
+// graph when the trigger fires, so a step without a rebuild is two kernels
+// and no conditional node (a conditional node and its set-condition kernel
+// cost about 12 us per step on this GB300); the conditional form where this
+// device refuses device-launched graphs.  Cell lists: the rebuild and the
+// step, every step.  Kinds without lists: the step alone.
+static int build_graph_on(spss_ctx *ctx, int stepper, const FastParams &P, int sampling, GraphEntry &g,
+                          unsigned long long launches0)
+{
+  FastPath *f = ctx->fast;
+  const bool trigger = f->kind == KIND_VERLET || f->trigger_only;
+  if (trigger && f->device_rebuild)
+  {
+    const int rc = build_device_rebuild(ctx, P, g);
+    if (rc != SPSS_OK)
+    {
+      // this device or driver refuses device-launched graphs: conditional form
+      cudaGetLastError();
+      g.release();
+      f->device_rebuild = false;
+      ctx->launches = launches0;
+    }
+  }
+  if (trigger && !f->device_rebuild) return build_graph_conditional(ctx, stepper, P, sampling, g, launches0);
+  const unsigned long long launches_step = ctx->launches;
+  cudaGraph_t graph = nullptr;
+  SPSS_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
+  int rc = SPSS_OK;
+  if (f->kind == KIND_CELLS)
+  {
+    const unsigned long long before = ctx->launches;
+    rc = launch_rebuild(ctx, P);
+    g.per_rebuild = 0;
+    (void) before;
+  }
+  if (rc == SPSS_OK) rc = launch_step(ctx, stepper, P, trigger ? g.rebuild_exec : nullptr);
+  if (rc == SPSS_OK && sampling) rc = launch_sampling(ctx, P, 1);
+  const cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+  if (rc != SPSS_OK)
+  {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  SPSS_CUDA_TRY(e);
+  g.graph = graph;
+  SPSS_CUDA_TRY(cudaGraphInstantiate(&g.exec, graph, 0));
+  g.per_step = (int) (ctx->launches - launches_step);
+  g.form = trigger ? GRAPH_DEVICE : (f->kind == KIND_CELLS ? GRAPH_ALWAYS : GRAPH_NONE);
   ctx->launches = launches0;  // captured, not launched
   return SPSS_OK;
 }
@@ -2806,7 +2947,14 @@ static int run_steps(spss_ctx *ctx, int stepper, double dt, long nsteps, int sam
     SPSS_TRY(build_graph(ctx, stepper, dt, sampling, g));
     it = f->graphs.emplace(key, g).first;
   }
-  const int rebuilds0 = f->h_ctrl->rebuilds;
+  int rebuilds0 = f->h_ctrl->rebuilds;
+  if ((it->second.form == GRAPH_DEVICE || it->second.form == GRAPH_NONE) && f->h_ctrl->rebuild)
+  {
+    // a rebuild pending before the first step (host request, eager steps):
+    // these graphs rebuild only after a step's trigger
+    SPSS_TRY(launch_rebuild(ctx, params(ctx, dt)));
+    rebuilds0 += 1;
+  }
   for (long k = 0; k < nsteps; ++k) SPSS_CUDA_TRY(cudaGraphLaunch(it->second.exec, ctx->stream));
   const int rc = sync_control(ctx);
   ctx->launches += (unsigned long long) nsteps * it->second.per_step
