@@ -3089,8 +3089,9 @@ static int take_snapshot(spss_ctx *ctx)
   return SPSS_OK;
 }
 
-// Back to the snapshot; the lists are rebuilt before the next step.
-static int restore_snapshot(spss_ctx *ctx)
+// Back to the snapshot; the lists are rebuilt before the next step.  `keep`:
+// the snapshot stays for another restore.
+static int restore_snapshot(spss_ctx *ctx, bool keep = false)
 {
   FastPath *f = ctx->fast;
   Snapshot &S = f->snap;
@@ -3116,13 +3117,14 @@ static int restore_snapshot(spss_ctx *ctx)
   ctx->step_counter = f->h_ctrl->step;
   ctx->accumulated_displacement = f->h_ctrl->acc;
   ctx->should_update_lists = 1;
-  S.release();
+  if (!keep) S.release();
   return SPSS_OK;
 }
 
 // Times `steps` steps (graph launches, CUDA events) for every tile width and
-// launch form, keeps the fastest and puts the state back as it was.  The
-// step results do not depend on the tiling.
+// launch form, each from the state the call found, keeps the fastest and
+// puts the state back as it was.  The step results do not depend on the
+// tiling.
 int fast_autotune(spss_ctx *ctx, int stepper, double dt, int steps, double *best_ms)
 {
   FastPath *f = ctx->fast;
@@ -3143,6 +3145,13 @@ int fast_autotune(spss_ctx *ctx, int stepper, double dt, int steps, double *best
   for (int w : widths)
     for (int pers = 0; pers <= 1 && rc == SPSS_OK; ++pers)
     {
+      // every candidate from the same state: a list rebuild that the trigger
+      // calls for inside the timed steps falls on the same step for all of
+      // them (results do not depend on the tiling), not on whichever
+      // candidate happens to be running when the accumulated displacement
+      // reaches the skin
+      rc = restore_snapshot(ctx, true);
+      if (rc != SPSS_OK) break;
       f->persistent = pers;
       rc = set_tiling(ctx, w);
       if (rc == SPSS_OK) rc = run_steps(ctx, stepper, dt, 2, 0);  // builds the graph, warms up
