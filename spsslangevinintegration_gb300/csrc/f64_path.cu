@@ -25,6 +25,7 @@ struct F64Path
       scratch_knext;
   DeviceArray<int> cell_of;
   DeviceArray<float2> posf;  // stage positions wrapped into the box, float (all-pairs range pre-test)
+  DeviceArray<double2> csphi;  // cos and sin of the stage phase (all pairs: written with the stage)
   Binner binner;
   int cells_nc = 0;  // cells per side of the last build (0: none)
   DeviceArray<int> vl_count, vl_off, vl_ent;
@@ -186,14 +187,17 @@ __device__ __forceinline__ void add_pair(const K64 &k, Sums &a, double phi_i, do
 
 // Output of one particle (ParticleSystemFirstOrder.cpp:220-226, ParticleSystemSecondOrder.cpp:166-175);
 // the torque component is left untouched when the particle has no neighbour.
-__device__ __forceinline__ void write_k(const K64 &k, int i, const double *st, Sums a, double *k_next, double *caf)
+// `cs`: cos and sin of the particle's phase computed beforehand (the same
+// functions of the same value), or null.
+__device__ __forceinline__ void write_k(const K64 &k, int i, const double *st, Sums a, double *k_next, double *caf,
+                                        const double2 *cs = nullptr)
 {
   const long ii = (long) k.s * i;
   if (k.model == 1)
   {
     const double phi_i = st[2], omega_i = st[3];
-    k_next[ii] = k.v0 * cos(phi_i);
-    k_next[ii + 1] = k.v0 * sin(phi_i);
+    k_next[ii] = k.v0 * (cs ? cs->x : cos(phi_i));
+    k_next[ii + 1] = k.v0 * (cs ? cs->y : sin(phi_i));
     k_next[ii + 2] = omega_i;
     if (a.card != 0.0)
     {
@@ -205,8 +209,8 @@ __device__ __forceinline__ void write_k(const K64 &k, int i, const double *st, S
     const double v_x_i = st[2], v_y_i = st[3], phi_i = st[4], omega_i = st[5];
     k_next[ii] = v_x_i;
     k_next[ii + 1] = v_y_i;
-    k_next[ii + 2] = -k.xi_r * v_x_i + k.v0 * cos(phi_i);
-    k_next[ii + 3] = -k.xi_r * v_y_i + k.v0 * sin(phi_i);
+    k_next[ii + 2] = -k.xi_r * v_x_i + k.v0 * (cs ? cs->x : cos(phi_i));
+    k_next[ii + 3] = -k.xi_r * v_y_i + k.v0 * (cs ? cs->y : sin(phi_i));
     k_next[ii + 4] = omega_i;
     if (a.card != 0.0)
     {
@@ -237,10 +241,13 @@ __global__ void f64_cell_kernel(K64 k, const double *__restrict__ rk, int nc, in
 }
 
 // The stage state of one particle per thread (the same expression as
-// f64_stage_kernel, element by element) and its position wrapped into the
-// unit box as floats, for the all-pairs range pre-test.
+// f64_stage_kernel, element by element), its position wrapped into the
+// unit box as floats, for the all-pairs range pre-test, and the cos and sin
+// of its phase for its own derivative (one thread per particle here, where
+// the pair kernel would spend a whole warp's FP64 pipe time on one lane).
 __global__ void f64_stage_posf_kernel(K64 k, const double *__restrict__ st, const double *__restrict__ kp,
-                                      double *__restrict__ rk, float2 *__restrict__ posf, double k_coef, double dt)
+                                      double *__restrict__ rk, float2 *__restrict__ posf,
+                                      double2 *__restrict__ csphi, double k_coef, double dt)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= k.n) return;
@@ -248,6 +255,8 @@ __global__ void f64_stage_posf_kernel(K64 k, const double *__restrict__ st, cons
   for (int q = 0; q < k.s; ++q) rk[ii + q] = st[ii + q] + k_coef * dt * kp[ii + q];
   const double x = rk[ii], y = rk[ii + 1];
   posf[i] = make_float2((float) (x - floor(x)), (float) (y - floor(y)));
+  const double phi = rk[ii + (k.model == 1 ? 2 : 4)];
+  csphi[i] = make_double2(cos(phi), sin(phi));
 }
 
 // A lower bound of the minimum-image distance of two particles from their
@@ -270,7 +279,8 @@ __device__ __forceinline__ bool pretest_out(const K64 &k, float2 a, float2 b)
 // range; every other pair is decided by the reference's FP64 expression, so
 // the neighbour sets are the FP64 ones.
 __global__ void f64_allpairs_kernel(K64 k, const double *__restrict__ rk, const float2 *__restrict__ posf,
-                                    double *__restrict__ k_next, double *__restrict__ caf)
+                                    const double2 *__restrict__ csphi, double *__restrict__ k_next,
+                                    double *__restrict__ caf)
 {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -288,7 +298,12 @@ __global__ void f64_allpairs_kernel(K64 k, const double *__restrict__ rk, const 
   const float2 pi = posf[i];
   Sums a{0.0, 0.0, 0.0};
   // the lane's candidates j = lane, lane + 32, ... in that order; the float
-  // positions of four of them are loaded together
+  // positions of four of them are loaded together.  The pair terms (FP64 sin
+  // and cos, a warp's full FP64 pipe time whatever the lanes) wait until the
+  // scan is over, so the few neighbours of a particle, found by different
+  // lanes in different iterations, are summed in one pass; each lane still
+  // adds its own neighbours in ascending j, so the sums are unchanged.
+  int pend[4], np = 0;
   for (int j0 = lane; j0 < k.n; j0 += 128)
   {
     float2 pj[4];
@@ -300,8 +315,25 @@ __global__ void f64_allpairs_kernel(K64 k, const double *__restrict__ rk, const 
       const int j = j0 + 32 * u;
       if (j >= k.n || j == i || pretest_out(k, pi, pj[u])) continue;
       const double *sj = rk + (long) k.s * j;
-      if (pair_dr2<false>(k, x_i, y_i, sj[0], sj[1]) <= k.rho2) add_pair(k, a, phi_i, omega_i, sj[ip], sj[ip + 1]);
+      if (pair_dr2<false>(k, x_i, y_i, sj[0], sj[1]) <= k.rho2)
+      {
+        if (np == 4)
+        {
+          for (int t = 0; t < 4; ++t)
+          {
+            const double *sp = rk + (long) k.s * pend[t];
+            add_pair(k, a, phi_i, omega_i, sp[ip], sp[ip + 1]);
+          }
+          np = 0;
+        }
+        pend[np++] = j;
+      }
     }
+  }
+  for (int t = 0; t < np; ++t)
+  {
+    const double *sp = rk + (long) k.s * pend[t];
+    add_pair(k, a, phi_i, omega_i, sp[ip], sp[ip + 1]);
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1)
@@ -310,7 +342,7 @@ __global__ void f64_allpairs_kernel(K64 k, const double *__restrict__ rk, const 
     a.card += __shfl_xor_sync(0xffffffffu, a.card, off);
     a.caf += __shfl_xor_sync(0xffffffffu, a.caf, off);
   }
-  if (lane == 0) write_k(k, i, st, a, k_next, caf);
+  if (lane == 0) write_k(k, i, st, a, k_next, caf, csphi + i);
 }
 
 // Linked list (ParticleSystemFirstOrder.cpp:231-353, ParticleSystemSecondOrder.cpp:276-409).
@@ -636,6 +668,7 @@ int f64_create(spss_ctx *ctx)
   SPSS_TRY(f->nat_freq.reserve(ctx->p.n));
   SPSS_TRY(f->cell_of.reserve(ctx->p.n));
   SPSS_TRY(f->posf.reserve(ctx->p.n));
+  SPSS_TRY(f->csphi.reserve(ctx->p.n));
   SPSS_TRY(f->vl_count.reserve(ctx->p.n));
   SPSS_TRY(f->vl_off.reserve(ctx->p.n + 1));
   SPSS_TRY(f->max2.reserve(1));
@@ -665,6 +698,7 @@ void f64_destroy(spss_ctx *ctx)
   f->scratch_knext.release();
   f->cell_of.release();
   f->posf.release();
+  f->csphi.release();
   if (f->rk4_exec) cudaGraphExecDestroy(f->rk4_exec);
   if (f->rk4_graph) cudaGraphDestroy(f->rk4_graph);
   f->binner.release();
@@ -762,7 +796,7 @@ int f64_evaluate(spss_ctx *ctx, int variant, const double *d_state, const double
   const int tb = 256;
   if (variant == SPSS_VARIANT_ALL_PAIRS)
     f64_stage_posf_kernel<<<blocks_for(k.n, tb), tb, 0, ctx->stream>>>(k, d_state, d_kprev, f->rk.ptr, f->posf.ptr,
-                                                                       k_coef, dt);
+                                                                       f->csphi.ptr, k_coef, dt);
   else
     f64_stage_kernel<<<blocks_for(len, tb), tb, 0, ctx->stream>>>(d_state, d_kprev, f->rk.ptr, len, k_coef, dt);
   ++ctx->launches;
@@ -771,8 +805,8 @@ int f64_evaluate(spss_ctx *ctx, int variant, const double *d_state, const double
   switch (variant)
   {
     case SPSS_VARIANT_ALL_PAIRS:
-      f64_allpairs_kernel<<<blocks_for(32L * k.n, 128), 128, 0, ctx->stream>>>(k, f->rk.ptr, f->posf.ptr, d_knext,
-                                                                                f->caf.ptr);
+      f64_allpairs_kernel<<<blocks_for(32L * k.n, 128), 128, 0, ctx->stream>>>(k, f->rk.ptr, f->posf.ptr,
+                                                                                f->csphi.ptr, d_knext, f->caf.ptr);
       ++ctx->launches;
       return check_launch("f64_allpairs_kernel");
     case SPSS_VARIANT_LINKED_LIST:
