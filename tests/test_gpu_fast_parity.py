@@ -360,3 +360,64 @@ def test_verlet_radius_over_a_third_runs_all_pairs_with_the_trigger(variant, ste
     err = state_err(got, x, 4).max(axis=1)
     assert np.quantile(err, 0.999) <= 1e-3
     assert np.median(err) <= 1e-5
+
+
+def _verlet_context(n, seed=3):
+    p = params(2, n)
+    r_max = 1.3 * p["rho"]
+    return gpu_context(p, precision=F32, variant=4, r_max=r_max, nc_verlet=int(1 / r_max), seed=seed), p
+
+
+def test_graph_step_whose_trigger_fires_reports_it_like_single_steps():
+    """A graph step whose displacement trigger fires rebuilds the lists at once
+    (the control kernel tail-launches the rebuild graph); single steps rebuild
+    at the start of the next step.  Both report should_update_lists after
+    that step, as the reference does, and continue with the same bits."""
+    n = 12000
+    ctx, p = _verlet_context(n)
+    x0 = initial(2, n, 6, v=p["v0"])
+    with ctx:
+        ctx.set_state(x0)
+        ctx.step(2, 0.005, 0.005)  # the first rebuild
+        m = 1
+        while ctx.verlet_state()[1] == 0 and m < 400:
+            ctx.step(2, (m + 1) * 0.005, 0.005)
+            m += 1
+        assert ctx.verlet_state()[1] == 1, "the trigger should fire within 400 steps"
+        eager_flag_state = (ctx.get_state(), ctx.verlet_state())
+        for k in range(30):
+            ctx.step(2, (m + k + 1) * 0.005, 0.005)
+        eager_end = ctx.get_state()
+    ctx, _ = _verlet_context(n)
+    with ctx:
+        ctx.set_state(x0)
+        ctx.steps(2, 0.0, 0.005, m)
+        builds = ctx.rebuild_count
+        np.testing.assert_array_equal(ctx.get_state(), eager_flag_state[0])
+        assert ctx.verlet_state() == eager_flag_state[1]
+        ctx.steps(2, 0.0, 0.005, 30)
+        np.testing.assert_array_equal(ctx.get_state(), eager_end)
+        assert ctx.rebuild_count >= builds
+
+
+def test_host_requested_rebuild_runs_before_the_next_graph_step():
+    """spss_set_should_update_lists(1) between graph runs rebuilds the lists
+    before the next step; the neighbours within rho are the same, so the run
+    differs from the unforced one only in the order of the sums (the slot
+    order within cells changes with the extra re-sort)."""
+    n = 12000
+    ctx, p = _verlet_context(n)
+    x0 = initial(2, n, 7, v=p["v0"])
+    with ctx:
+        ctx.set_state(x0)
+        ctx.steps(2, 0.0, 0.005, 5)
+        before = ctx.rebuild_count
+        ctx.set_should_update_lists(1)
+        ctx.steps(2, 0.0, 0.005, 5)
+        assert ctx.rebuild_count >= before + 1
+        forced = ctx.get_state()
+    ctx, _ = _verlet_context(n)
+    with ctx:
+        ctx.set_state(x0)
+        ctx.steps(2, 0.0, 0.005, 10)
+        assert state_err(forced, ctx.get_state(), 6).max() <= 1e-5
