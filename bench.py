@@ -15,9 +15,9 @@ HBM (CUDA events on the library's stream, max over ranks, summed over ranks).
 `e2e`: the same through spss_step_host (host array in, host array out every
 step, the host array page-locked).  `roofline`: the pair-and-update kernel's
 algorithmic bytes over its CUDA-event duration.  `cpu_baseline` (rank 0): the oracle port of the
-reference algorithm on this host's cores.  `config1`, `config2`: the two
-smaller benchmark configurations (first order N = 1000 all pairs RK4 FP64;
-second order N = 65,536 cell list SE) next to the oracle port.  `cells`: the
+reference algorithm on this host's cores.  `allpairs_rk4_n1000`,
+`cells_se_n65536`: two smaller workloads (first order N = 1000 all pairs RK4
+FP64; second order N = 65,536 cell list SE) next to the oracle port.  `cells`: the
 same workload with cell lists rebuilt every step (the reference's linked
 list) next to the oracle port of that cell-list workload.  `sweep`: 512
 independent systems of the batched parameter sweep stepped as one batch with
@@ -238,14 +238,14 @@ def first_order_initial(n, seed):
 
 
 def run_config_legs(args, rank, world, barrier, max_over_ranks):
-    """The two smaller benchmark configurations next to the oracle port of the
-    same workload on this host's cores:
-      1. first order, N = 1000, density 1, all pairs called directly, RK4,
-         D = 0, v0 = 0.1, sigma = 1, dt = 0.01, FP64 (the reference's
-         arithmetic path), the configuration's 1000 steps;
-      2. second order, N = 65,536, density 2, cell list, StochasticEuler,
-         D = 0.1, m = 1, v0 = 0.5, dt = 0.005, FP32 (GB300 path), 2000 of the
-         configuration's 10,000 steps."""
+    """Two smaller workloads next to the oracle port of the same workload on
+    this host's cores:
+      allpairs_rk4_n1000: first order, N = 1000, density 1, all pairs called
+         directly, RK4, D = 0, v0 = 0.1, sigma = 1, dt = 0.01, FP64 (the
+         reference's arithmetic path), a run of 1000 steps;
+      cells_se_n65536: second order, N = 65,536, density 2, cell list,
+         StochasticEuler, D = 0.1, m = 1, v0 = 0.5, dt = 0.005, FP32 (GB300
+         path), 2000 steps of a 10,000-step run timed."""
     import torch
 
     from oracle import binding as ob
@@ -255,8 +255,9 @@ def run_config_legs(args, rank, world, barrier, max_over_ranks):
     out = {}
     cores = os.cpu_count() or 1
     ob.set_threads(cores, bench=True)
-    cases = (("config1", 1, 1000, 1.0, 0.1, 0.0, RK4, ALL_PAIRS, PRECISION_F64, 0.01, 1000, 1000),
-             ("config2", 2, 65536, 2.0, 0.5, 0.1, STOCHASTIC_EULER, LINKED_LIST, PRECISION_F32, DT, 2000, 10000))
+    cases = (("allpairs_rk4_n1000", 1, 1000, 1.0, 0.1, 0.0, RK4, ALL_PAIRS, PRECISION_F64, 0.01, 1000, 1000),
+             ("cells_se_n65536", 2, 65536, 2.0, 0.5, 0.1, STOCHASTIC_EULER, LINKED_LIST, PRECISION_F32, DT, 2000,
+              10000))
     for name, model, n, density, v0, D, stepper, variant, precision, dt, steps, full in cases:
         rho, kw, L = config_system(model, n, density, v0, D=D)
         x0 = first_order_initial(n, rank) if model == 1 else initial_state(n, L, rank)
@@ -279,7 +280,7 @@ def run_config_legs(args, rank, world, barrier, max_over_ranks):
                      "all pairs" if variant == ALL_PAIRS else "cell list",
                      "RK4, D=0, v0=0.1, sigma=1 (FP64 path)" if model == 1 else
                      "StochasticEuler, D=0.1, m=1, v0=0.5, sigma=1 (FP32 path)", dt,
-                     "%d of the configuration's %d steps timed" % (steps, full)),
+                     "%d steps of a %d-step run timed" % (steps, full)),
                  "value": n * steps * world / el, "unit": "particle-steps/s", "ms_per_step": 1e3 * el / steps,
                  "steps_timed": steps, "gpu_launches_per_step": launches / steps,
                  "timing": "wall clock around %d steps (graph launches where the path has them, one host "
@@ -382,7 +383,7 @@ def run_sweep_leg(args, rank, world, barrier, max_over_ranks, verlet=False):
     """Batched parameter sweep: 512 independent systems in one batch context
     (one CUDA graph per step for all systems), tiling picked by the autotuner;
     phase-diagram points per hour at 20,000 steps per point.  Cell lists
-    rebuilt every step (the configuration's choice), or with `verlet` the
+    rebuilt every step (the sweep's prescribed method), or with `verlet` the
     reference's linked list + Verlet routine with skin 0.3 R, each system's
     lists rebuilt when its own displacement trigger fires (the same neighbour
     sets within R)."""
@@ -553,7 +554,7 @@ def run_reference(args, rank, world):
 
 
 def run_legs_only(args, rank, world, local_rank):
-    """Only the configuration, cell-list, sweep, Verlet-sweep and/or surrogate
+    """Only the smaller-workload, cell-list, sweep, Verlet-sweep and/or surrogate
     legs (for profiling them alone); the default run measures every leg."""
     import torch
 
