@@ -258,6 +258,13 @@ int spss_batch_reset_stats(spss_ctx *ctx);
  * on the tiling; the lists are rebuilt before the next step.  F32 contexts. */
 int spss_set_tiling(spss_ctx *ctx, int tile_cells, int persistent);
 int spss_get_tiling(spss_ctx *ctx, int *tile_cells, int *persistent);
+/* How steps run as CUDA graphs (spss_steps, spss_batch_run) rebuild Verlet
+ * lists: 1 (default) the step's control kernel launches the rebuild as a
+ * device graph when the trigger fires; 0 a conditional graph node holds the
+ * rebuild at the start of each step (the form used where the device refuses
+ * device-launched graphs; about 12 us more per step on GB300).  Results are
+ * identical.  F32 contexts.  No counterpart in the reference. */
+int spss_set_device_rebuild(spss_ctx *ctx, int enabled);
 /* Times `steps` steps of every tiling candidate (16 to 64 cells per tile in steps of 4,
  * both launch forms) on the context's current state, keeps the fastest and
  * restores the state, step counter and trigger as they were (the lists are

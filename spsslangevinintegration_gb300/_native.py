@@ -101,6 +101,7 @@ SIGNATURES = {
     "spss_batch_reset_stats": (_i, [_vp]),
     "spss_set_tiling": (_i, [_vp, _i, _i]),
     "spss_get_tiling": (_i, [_vp, _ip, _ip]),
+    "spss_set_device_rebuild": (_i, [_vp, _i]),
     "spss_autotune": (_i, [_vp, _i, _d, _i, _dp]),
     "spss_frame_async": (_i, [_vp, _i, _fp, _l]),
     "spss_integrate_dopri5": (_i, [_vp, _d, _d, _d, _d, _d, _vp, _vp, P(_l)]),

@@ -281,6 +281,11 @@ class Context:
         N.check(self.L.spss_get_tiling(self.h, ctypes.byref(tc), ctypes.byref(pers)), "spss_get_tiling")
         return tc.value, bool(pers.value)
 
+    def set_device_rebuild(self, enabled):
+        """Graph-driven steps rebuild lists through a device-launched graph (True, default) or
+        under a conditional graph node (False); results are identical."""
+        N.check(self.L.spss_set_device_rebuild(self.h, int(bool(enabled))), "spss_set_device_rebuild")
+
     def autotune(self, stepper, dt, steps=5):
         """Fastest tiling over trial steps; the state is restored.  Returns ms per step."""
         ms = ctypes.c_double()

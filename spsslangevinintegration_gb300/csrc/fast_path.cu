@@ -2866,8 +2866,9 @@ static int build_device_rebuild(spss_ctx *ctx, const FastParams &P, GraphEntry &
 // graph when the trigger fires, so a step without a rebuild is two kernels
 // and no conditional node (a conditional node and its set-condition kernel
 // cost about 12 us per step on this GB300); the conditional form where this
-// device refuses device-launched graphs.  Cell lists: the rebuild and the
-// step, every step.  Kinds without lists: the step alone.
+// device refuses device-launched graphs (or when spss_set_device_rebuild
+// asks for it, for every kind).  Cell lists: the rebuild and the step, every
+// step.  Kinds without lists: the step alone.
 static int build_graph_on(spss_ctx *ctx, int stepper, const FastParams &P, int sampling, GraphEntry &g,
                           unsigned long long launches0)
 {
@@ -2885,7 +2886,7 @@ static int build_graph_on(spss_ctx *ctx, int stepper, const FastParams &P, int s
       ctx->launches = launches0;
     }
   }
-  if (trigger && !f->device_rebuild) return build_graph_conditional(ctx, stepper, P, sampling, g, launches0);
+  if (!f->device_rebuild) return build_graph_conditional(ctx, stepper, P, sampling, g, launches0);
   const unsigned long long launches_step = ctx->launches;
   cudaGraph_t graph = nullptr;
   SPSS_CUDA_TRY(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed));
@@ -3043,6 +3044,16 @@ int fast_set_tiling(spss_ctx *ctx, int tile_cells, int persistent)
   FastPath *f = ctx->fast;
   f->persistent = persistent;
   return set_tiling(ctx, tile_cells);
+}
+
+int fast_set_device_rebuild(spss_ctx *ctx, int enabled)
+{
+  FastPath *f = ctx->fast;
+  if (f->device_rebuild == (enabled != 0)) return SPSS_OK;
+  f->device_rebuild = enabled != 0;
+  for (auto &g : f->graphs) g.second.release();
+  f->graphs.clear();
+  return SPSS_OK;
 }
 
 int fast_get_tiling(spss_ctx *ctx, int *tile_cells, int *persistent)

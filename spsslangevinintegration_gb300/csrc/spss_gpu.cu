@@ -850,6 +850,13 @@ int spss_get_tiling(spss_ctx *ctx, int *tile_cells, int *persistent)
   return fast_get_tiling(ctx, tile_cells, persistent);
 }
 
+int spss_set_device_rebuild(spss_ctx *ctx, int enabled)
+{
+  if (!ctx) return SPSS_ERR_INVALID_ARGUMENT;
+  if (is_f64(ctx)) return SPSS_ERR_NOT_SUPPORTED;
+  return fast_set_device_rebuild(ctx, enabled);
+}
+
 int spss_autotune(spss_ctx *ctx, int stepper, double dt, int steps, double *best_ms_per_step)
 {
   if (!ctx) return SPSS_ERR_INVALID_ARGUMENT;

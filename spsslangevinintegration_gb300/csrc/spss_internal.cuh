@@ -333,6 +333,7 @@ int fast_apply_pbc(spss_ctx *ctx);
 
 int fast_set_tiling(spss_ctx *ctx, int tile_cells, int persistent);
 int fast_get_tiling(spss_ctx *ctx, int *tile_cells, int *persistent);
+int fast_set_device_rebuild(spss_ctx *ctx, int enabled);
 int fast_autotune(spss_ctx *ctx, int stepper, double dt, int steps, double *best_ms);
 int fast_system_order_parameters(spss_ctx *ctx, double *h_out);
 int fast_batch_run(spss_ctx *ctx, int stepper, double dt, long nsteps, long sample_every, long sample_from);

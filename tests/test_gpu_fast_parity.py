@@ -421,3 +421,24 @@ def test_host_requested_rebuild_runs_before_the_next_graph_step():
         ctx.set_state(x0)
         ctx.steps(2, 0.0, 0.005, 10)
         assert state_err(forced, ctx.get_state(), 6).max() <= 1e-5
+
+
+@pytest.mark.parametrize("variant,stepper", [(4, 2), (2, 1)])
+def test_conditional_graph_form_equals_device_rebuild(variant, stepper):
+    """The conditional-node step graph (the form for devices that refuse
+    device-launched graphs) steps bit for bit as the default form, through
+    list rebuilds (Verlet) and per-step cell lists."""
+    n = 12000
+    p = params(2, n)
+    r_max = 1.3 * p["rho"]
+    x0 = initial(2, n, 8, v=p["v0"])
+    out = []
+    for device in (True, False):
+        with gpu_context(p, precision=F32, variant=variant, r_max=r_max, nc_verlet=int(1 / r_max), seed=4) as ctx:
+            ctx.set_device_rebuild(device)
+            ctx.set_state(x0)
+            ctx.steps(stepper, 0.0, 0.005, 150)
+            out.append((ctx.get_state(), ctx.verlet_state(), ctx.rebuild_count))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    assert out[0][1] == out[1][1]
+
