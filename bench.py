@@ -13,7 +13,8 @@ field), mapped to the reference's unit box (L = sqrt(N / density)).
 Prints one JSON line.  `value`: particle-steps/s with the state resident in
 HBM (CUDA events on the library's stream, max over ranks, summed over ranks).
 `e2e`: the same through spss_step_host (host array in, host array out every
-step, the host array page-locked).  `roofline`: the pair-and-update kernel's
+step, the host array page-locked), with `e2e.link` the host link's floor
+under it (copy-engine copies of the same bytes).  `roofline`: the pair-and-update kernel's
 algorithmic bytes over its CUDA-event duration.  `cpu_baseline` (rank 0): the oracle port of the
 reference algorithm on this host's cores.  `allpairs_rk4_n1000`,
 `cells_se_n65536`: two smaller workloads (first order N = 1000 all pairs RK4
@@ -160,6 +161,33 @@ def traffic_per_launch():
         return float(d["dram_bytes_per_particle"])
     except (OSError, KeyError, ValueError):
         return None
+
+
+def host_link_ms(nbytes, reps=5):
+    """Median times (ms) of copy-engine copies of `nbytes` from page-locked
+    host memory to the device and back (CUDA events on torch's stream): the
+    host link's floor under the end-to-end figure, whose upload and download
+    kernels move the same bytes over the same link."""
+    import torch
+
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = []
+    for src, dst in ((h, d), (d, h)):
+        for _ in range(2):
+            dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        out.append(statistics.median(ts))
+    del h, d
+    return out
 
 
 def cpu_baseline(n, budget_s=20.0, bench_lib=True):
@@ -715,6 +743,8 @@ def run_ours(args, rank, world, local_rank):
     e2e_s = max_over_ranks(e2e_s + e2e_added * rebuild_ms * 1e-3)
     e2e_value = world * n * e2e_steps / e2e_s
     pinned.free()
+    h2d_ms, d2h_ms = host_link_ms(n * 6 * 8)
+    link_floor_ms = h2d_ms + d2h_ms + ms / args.steps
     acc, flag, uses = ctx.verlet_state()
     ctx.close()
 
@@ -747,7 +777,12 @@ def run_ours(args, rank, world, local_rank):
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": n * 6 * 8,
                 "d2h_bytes_per_step": n * 6 * 8, "steps": e2e_steps, "rebuilds_added": e2e_added,
                 "path": "spss_step_host: host AoS float64 in, one SRK step, host AoS out (page-locked host "
-                        "array from spss_pinned_alloc)"},
+                        "array from spss_pinned_alloc)",
+                "link": {"h2d_ms": h2d_ms, "d2h_ms": d2h_ms, "h2d_gbs": n * 48 / h2d_ms / 1e6,
+                         "d2h_gbs": n * 48 / d2h_ms / 1e6, "floor_ms_per_step": link_floor_ms,
+                         "frac": link_floor_ms / (e2e_s * 1e3 / e2e_steps),
+                         "how": "copy-engine copies of one step's state bytes each way (page-locked host memory, "
+                                "CUDA events) plus ms_per_step: the host link's floor under the end-to-end step"}},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
         "verlet": {"accumulated_displacement": acc, "rebuild_pending": flag},

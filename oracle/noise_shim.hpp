@@ -10,7 +10,7 @@
  *  DynamicalSystems/ParticleSystemSecondOrder.cpp:443,447-449).
  * After <random> is included, `normal_distribution` is redefined to a
  * distribution that ignores the generator and returns the next value of a
- * replay buffer filled by the driver.  The GPU writes that buffer from the
+ * replay buffer filled by ref_driver.cpp.  The GPU writes that buffer from the
  * exact normals its Philox stream produced, so the oracle and the GPU see
  * identical noise in the reference's draw order.
  *
