@@ -2770,8 +2770,11 @@ int fast_step(spss_ctx *ctx, int stepper, double t, double dt)
 static int build_graph_on(spss_ctx *ctx, int stepper, const FastParams &P, int sampling, GraphEntry &g,
                           unsigned long long launches0);
 
-// One step as a graph: rebuild under a conditional node, then step + control
-// (+ the gated order-parameter sample).
+// One step as a graph (+ the gated order-parameter sample): on a rebuild
+// trigger, step + control, the control kernel tail-launching the rebuild graph
+// when it is due (or the conditional form, whose rebuild sits under a
+// conditional node ahead of the step); with cell lists, rebuild + step +
+// control; otherwise step + control.
 static int build_graph(spss_ctx *ctx, int stepper, double dt, int sampling, GraphEntry &g)
 {
   const FastParams P = params(ctx, dt);
@@ -2893,10 +2896,8 @@ static int build_graph_on(spss_ctx *ctx, int stepper, const FastParams &P, int s
   int rc = SPSS_OK;
   if (f->kind == KIND_CELLS)
   {
-    const unsigned long long before = ctx->launches;
     rc = launch_rebuild(ctx, P);
     g.per_rebuild = 0;
-    (void) before;
   }
   if (rc == SPSS_OK) rc = launch_step(ctx, stepper, P, trigger ? g.rebuild_exec : nullptr);
   if (rc == SPSS_OK && sampling) rc = launch_sampling(ctx, P, 1);
