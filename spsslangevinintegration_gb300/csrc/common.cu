@@ -42,6 +42,7 @@ constexpr int kScanTile = kScanThreads * kScanItems;
 __global__ void scan_tile_kernel(const int *__restrict__ in, int *__restrict__ out, int *__restrict__ sums, int n)
 {
   __shared__ int warp_tot[kScanThreads / 32];
+  pdl_enter();
   const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
   int v[kScanItems];
   int local = 0;
@@ -91,18 +92,19 @@ __global__ void scan_tile_kernel(const int *__restrict__ in, int *__restrict__ o
 
 __global__ void scan_add_kernel(int *__restrict__ out, const int *__restrict__ block_off, int n, int nblocks)
 {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] += block_off[i / kScanTile];
   if (i == 0) out[n] = block_off[nblocks];
 }
 
-int Scanner::run(const int *in, int *out, int n, cudaStream_t stream, unsigned long long &launches)
+int Scanner::run(const int *in, int *out, int n, cudaStream_t stream, unsigned long long &launches, bool chained)
 {
-  return run_level(in, out, n, 0, stream, launches);
+  return run_level(in, out, n, 0, stream, launches, chained);
 }
 
 int Scanner::run_level(const int *in, int *out, int n, size_t level, cudaStream_t stream,
-                       unsigned long long &launches)
+                       unsigned long long &launches, bool chained)
 {
   if (n <= 0)
   {
@@ -112,7 +114,7 @@ int Scanner::run_level(const int *in, int *out, int n, size_t level, cudaStream_
   const int nblocks = (n + kScanTile - 1) / kScanTile;
   if (nblocks == 1)
   {
-    scan_tile_kernel<<<1, kScanThreads, 0, stream>>>(in, out, nullptr, n);
+    SPSS_CUDA_TRY(launch_chained(chained, scan_tile_kernel, 1, kScanThreads, 0, stream, in, out, (int *) nullptr, n));
     ++launches;
     return check_launch("scan_tile_kernel");
   }
@@ -121,11 +123,12 @@ int Scanner::run_level(const int *in, int *out, int n, size_t level, cudaStream_
   SPSS_TRY(levels[2 * level + 1].reserve(nblocks + 1));
   int *sums = levels[2 * level].ptr;       // device pointers stay valid if `levels` grows
   int *sums_off = levels[2 * level + 1].ptr;
-  scan_tile_kernel<<<nblocks, kScanThreads, 0, stream>>>(in, out, sums, n);
+  SPSS_CUDA_TRY(launch_chained(chained, scan_tile_kernel, nblocks, kScanThreads, 0, stream, in, out, sums, n));
   ++launches;
   SPSS_TRY(check_launch("scan_tile_kernel"));
-  SPSS_TRY(run_level(sums, sums_off, nblocks, level + 1, stream, launches));
-  scan_add_kernel<<<(n + 255) / 256, 256, 0, stream>>>(out, sums_off, n, nblocks);
+  SPSS_TRY(run_level(sums, sums_off, nblocks, level + 1, stream, launches, chained));
+  SPSS_CUDA_TRY(launch_chained(chained, scan_add_kernel, (n + 255) / 256, 256, 0, stream, out,
+                               (const int *) sums_off, n, nblocks));
   ++launches;
   return check_launch("scan_add_kernel");
 }
@@ -135,6 +138,7 @@ int Scanner::run_level(const int *in, int *out, int n, size_t level, cudaStream_
 __global__ void bin_count_kernel(const int *__restrict__ cell_of, int n, int *__restrict__ count,
                                  int *__restrict__ slot)
 {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) slot[i] = atomicAdd(&count[cell_of[i]], 1);
 }
@@ -142,6 +146,7 @@ __global__ void bin_count_kernel(const int *__restrict__ cell_of, int n, int *__
 __global__ void bin_scatter_kernel(const int *__restrict__ cell_of, const int *__restrict__ slot,
                                    const int *__restrict__ offsets, int n, int *__restrict__ members)
 {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) members[offsets[cell_of[i]] + slot[i]] = i;
 }
@@ -154,6 +159,7 @@ constexpr int kSortRegs = 8;
 
 __global__ void bin_sort_kernel(const int *__restrict__ offsets, int ncell, int *__restrict__ members)
 {
+  pdl_enter();
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncell) return;
   const int b = offsets[c], e = offsets[c + 1];
@@ -191,7 +197,8 @@ __global__ void bin_sort_kernel(const int *__restrict__ offsets, int ncell, int 
   }
 }
 
-int Binner::run(const int *cell_of, int n, int ncell_in, cudaStream_t stream, unsigned long long &launches)
+int Binner::run(const int *cell_of, int n, int ncell_in, cudaStream_t stream, unsigned long long &launches,
+                bool chained)
 {
   ncell = ncell_in;
   SPSS_TRY(count.reserve(ncell));
@@ -200,14 +207,17 @@ int Binner::run(const int *cell_of, int n, int ncell_in, cudaStream_t stream, un
   SPSS_TRY(members.reserve(n));
   SPSS_CUDA_TRY(cudaMemsetAsync(count.ptr, 0, sizeof(int) * ncell, stream));
   const int tb = 256;
+  // the count follows a memset: an ordinary launch
   bin_count_kernel<<<(n + tb - 1) / tb, tb, 0, stream>>>(cell_of, n, count.ptr, slot.ptr);
   ++launches;
   SPSS_TRY(check_launch("bin_count_kernel"));
-  SPSS_TRY(scanner.run(count.ptr, offsets.ptr, ncell, stream, launches));
-  bin_scatter_kernel<<<(n + tb - 1) / tb, tb, 0, stream>>>(cell_of, slot.ptr, offsets.ptr, n, members.ptr);
+  SPSS_TRY(scanner.run(count.ptr, offsets.ptr, ncell, stream, launches, chained));
+  SPSS_CUDA_TRY(launch_chained(chained, bin_scatter_kernel, (n + tb - 1) / tb, tb, 0, stream, cell_of,
+                               (const int *) slot.ptr, (const int *) offsets.ptr, n, members.ptr));
   ++launches;
   SPSS_TRY(check_launch("bin_scatter_kernel"));
-  bin_sort_kernel<<<(ncell + tb - 1) / tb, tb, 0, stream>>>(offsets.ptr, ncell, members.ptr);
+  SPSS_CUDA_TRY(launch_chained(chained, bin_sort_kernel, (ncell + tb - 1) / tb, tb, 0, stream,
+                               (const int *) offsets.ptr, ncell, members.ptr));
   ++launches;
   return check_launch("bin_sort_kernel");
 }

@@ -246,6 +246,9 @@ struct FastPath
   bool perm_valid = false;
   std::map<std::tuple<int, double, int>, GraphEntry> graphs;  // (stepper, dt, with sampling)
   bool device_rebuild = true;  // rebuilds tail-launched as device graphs (cleared if this device refuses)
+  // set while a cell-list step graph is captured: its kernels after the first
+  // are launched as a programmatic-dependent chain (each begins with pdl_enter)
+  bool chain = false;
   // per-system order parameters and their time averages
   DeviceArray<OrderSums> order_partial;
   DeviceArray<int2> order_items;   // (system, first slot) of every chunk, systems in order
@@ -578,6 +581,7 @@ __device__ __forceinline__ bool rebuilds_system(const FastBuffers &B, int sys)
 
 __global__ void fast_cells_kernel(FastParams P, FastBuffers B)
 {
+  pdl_enter();
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= P.n || B.ctrl->cells_fresh) return;  // the last step wrote every slot's cell id
   if (!rebuilds_system(B, B.sys_of[q]))
@@ -597,6 +601,7 @@ __global__ void fast_cells_kernel(FastParams P, FastBuffers B)
 // ascending old slot inside a cell).  Writes the other rec/aux buffer.
 __global__ void fast_permute_kernel(FastParams P, FastBuffers B)
 {
+  pdl_enter();
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= P.n) return;
   if (!rebuilds_system(B, B.sys_of[q])) return;  // its order is the identity
@@ -616,6 +621,7 @@ __global__ void fast_permute_kernel(FastParams P, FastBuffers B)
 // the systems left out keep their records where they are.
 __global__ void fast_copyback_kernel(FastParams P, FastBuffers B)
 {
+  pdl_enter();
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= P.n) return;
   if (!rebuilds_system(B, B.sys_of[q])) return;
@@ -634,6 +640,7 @@ __global__ void fast_copyback_kernel(FastParams P, FastBuffers B)
 // thread; runs before the tile layouts and list builds, which read them.
 __global__ void fast_after_permute_kernel(FastControl *ctrl, int permuted)
 {
+  pdl_enter();
   if (permuted && ctrl->rebuild != REBUILD_FLAGGED) ctrl->parity ^= 1;
   ctrl->cells_fresh = 0;  // the slots moved
 }
@@ -644,6 +651,7 @@ __global__ void fast_after_permute_kernel(FastControl *ctrl, int permuted)
 // rebuilt at each flagged rebuild).  One block.
 __global__ void fast_after_rebuild_kernel(FastControl *ctrl, SysControl *sysctl, int nsys)
 {
+  pdl_enter();
   for (int r = threadIdx.x; r < nsys; r += blockDim.x) sysctl[r].rebuild = 0;
   if (threadIdx.x == 0)
   {
@@ -813,6 +821,7 @@ __device__ void tile_layout(int t, int nc, int tc, const int *__restrict__ off, 
 // Layout of every tile of every system, once per rebuild.
 __global__ void fast_tile_layout_kernel(FastParams P, FastBuffers B)
 {
+  pdl_enter();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= P.ntiles) return;
   if (!rebuilds_system(B, B.tile_sys[t])) return;
@@ -1586,6 +1595,7 @@ __global__ void __launch_bounds__(kTileThreads, STEPPER == 2 ? 9
   __shared__ int list_staged, list_stride, self_base;
   __shared__ StencilRuns runs[KIND == KIND_CELLS ? kRunCells : 1];
   __shared__ unsigned char col_of[KIND == KIND_CELLS ? kTileCap : 4];
+  pdl_enter();
   FastControl *ctrl = B.ctrl;
   const int par = ctrl->parity;
   const uint4 *rin = par ? B.rec1 : B.rec0;
@@ -1675,6 +1685,7 @@ __global__ void __launch_bounds__(kTileThreads, 8) fast_tile_persistent_kernel(F
   __shared__ uint32_t phase;  // mbarrier phase of the next staged tile
   __shared__ StencilRuns runs[KIND == KIND_CELLS ? kRunCells : 1];
   __shared__ unsigned char col_of[KIND == KIND_CELLS ? kTileCap : 4];
+  pdl_enter();
   FastControl *ctrl = B.ctrl;
   const int par = ctrl->parity;
   const uint4 *rin = par ? B.rec1 : B.rec0;
@@ -1866,6 +1877,7 @@ __global__ void fast_control_kernel(FastControl *ctrl, SysControl *sysctl, const
                                     cudaGraphExec_t rebuild_exec)
 {
   __shared__ int any;
+  pdl_enter();
   if (threadIdx.x == 0) any = 0;
   __syncthreads();
   for (int r = threadIdx.x; r < nsys; r += blockDim.x)
@@ -2559,21 +2571,23 @@ static int launch_rebuild(spss_ctx *ctx, const FastParams &P)
     fast_cells_kernel<<<blocks_for(n, kTB), kTB, 0, ctx->stream>>>(P, B);
     ++ctx->launches;
     SPSS_TRY(check_launch("fast_cells_kernel"));
-    SPSS_TRY(f->binner.run(f->cell_of.ptr, n, f->total_cells, ctx->stream, ctx->launches));
+    SPSS_TRY(f->binner.run(f->cell_of.ptr, n, f->total_cells, ctx->stream, ctx->launches, f->chain));
     const FastBuffers B2 = buffers(ctx);  // binner buffers exist now
-    fast_permute_kernel<<<blocks_for(n, kTB), kTB, 0, ctx->stream>>>(P, B2);
+    SPSS_CUDA_TRY(launch_chained(f->chain, fast_permute_kernel, blocks_for(n, kTB), kTB, 0, ctx->stream, P, B2));
     ++ctx->launches;
     SPSS_TRY(check_launch("fast_permute_kernel"));
-    fast_copyback_kernel<<<blocks_for(n, kTB), kTB, 0, ctx->stream>>>(P, B2);
+    SPSS_CUDA_TRY(launch_chained(f->chain, fast_copyback_kernel, blocks_for(n, kTB), kTB, 0, ctx->stream, P, B2));
     ++ctx->launches;
     SPSS_TRY(check_launch("fast_copyback_kernel"));
   }
-  fast_after_permute_kernel<<<1, 1, 0, ctx->stream>>>(f->ctrl, has_cells(f->kind));
+  SPSS_CUDA_TRY(launch_chained(f->chain, fast_after_permute_kernel, 1, 1, 0, ctx->stream, f->ctrl,
+                               (int) has_cells(f->kind)));
   ++ctx->launches;
   SPSS_TRY(check_launch("fast_after_permute_kernel"));
   if (has_cells(f->kind))
   {
-    fast_tile_layout_kernel<<<blocks_for(f->ntiles, 128), 128, 0, ctx->stream>>>(P, buffers(ctx));
+    SPSS_CUDA_TRY(launch_chained(f->chain, fast_tile_layout_kernel, blocks_for(f->ntiles, 128), 128, 0, ctx->stream,
+                                 P, buffers(ctx)));
     ++ctx->launches;
     SPSS_TRY(check_launch("fast_tile_layout_kernel"));
   }
@@ -2583,7 +2597,8 @@ static int launch_rebuild(spss_ctx *ctx, const FastParams &P)
     ++ctx->launches;
     SPSS_TRY(check_launch("fast_verlet_tile_build_kernel"));
   }
-  fast_after_rebuild_kernel<<<1, 256, 0, ctx->stream>>>(f->ctrl, f->sysctl.ptr, f->nsys);
+  SPSS_CUDA_TRY(launch_chained(f->chain, fast_after_rebuild_kernel, 1, 256, 0, ctx->stream, f->ctrl, f->sysctl.ptr,
+                               f->nsys));
   ++ctx->launches;
   return check_launch("fast_after_rebuild_kernel");
 }
@@ -2591,16 +2606,20 @@ static int launch_rebuild(spss_ctx *ctx, const FastParams &P)
 template<int MODEL, int STEPPER, int KIND>
 static void launch_tiles(spss_ctx *ctx, const FastParams &P, const FastBuffers &B, int grid)
 {
+  const bool c = ctx->fast->chain;
   if (P.persistent)
   {
     if (P.nsys > 1)
-      fast_tile_persistent_kernel<MODEL, STEPPER, KIND, true><<<grid, kTileThreads, 0, ctx->stream>>>(P, B);
+      launch_chained(c, fast_tile_persistent_kernel<MODEL, STEPPER, KIND, true>, grid, kTileThreads, 0, ctx->stream, P, B);
     else
-      fast_tile_persistent_kernel<MODEL, STEPPER, KIND, false><<<grid, kTileThreads, 0, ctx->stream>>>(P, B);
+      launch_chained(c, fast_tile_persistent_kernel<MODEL, STEPPER, KIND, false>, grid, kTileThreads, 0, ctx->stream, P,
+                     B);
   } else
   {
-    if (P.nsys > 1) fast_tile_kernel<MODEL, STEPPER, KIND, true><<<grid, kTileThreads, 0, ctx->stream>>>(P, B);
-    else fast_tile_kernel<MODEL, STEPPER, KIND, false><<<grid, kTileThreads, 0, ctx->stream>>>(P, B);
+    if (P.nsys > 1)
+      launch_chained(c, fast_tile_kernel<MODEL, STEPPER, KIND, true>, grid, kTileThreads, 0, ctx->stream, P, B);
+    else
+      launch_chained(c, fast_tile_kernel<MODEL, STEPPER, KIND, false>, grid, kTileThreads, 0, ctx->stream, P, B);
   }
 }
 
@@ -2653,9 +2672,10 @@ static int launch_step(spss_ctx *ctx, int stepper, const FastParams &P, cudaGrap
                                                           P.always_rebuild, f->kind == KIND_VERLET || f->trigger_only,
                                                           P.selective, f->kind == KIND_CELLS ? 1 : 0, rebuild_exec);
   else
-    fast_control_kernel<false><<<1, 256, 0, ctx->stream>>>(f->ctrl, f->sysctl.ptr, f->sys.ptr, f->nsys,
-                                                           P.always_rebuild, f->kind == KIND_VERLET || f->trigger_only,
-                                                           P.selective, f->kind == KIND_CELLS ? 1 : 0, nullptr);
+    launch_chained(f->chain, fast_control_kernel<false>, 1, 256, 0, ctx->stream, f->ctrl, f->sysctl.ptr,
+                   (const SysParams *) f->sys.ptr, f->nsys, (int) P.always_rebuild,
+                   (int) (f->kind == KIND_VERLET || f->trigger_only), (int) P.selective,
+                   f->kind == KIND_CELLS ? 1 : 0, (cudaGraphExec_t) nullptr);
   ++ctx->launches;
   return check_launch("fast_control_kernel");
 }
@@ -2896,10 +2916,12 @@ static int build_graph_on(spss_ctx *ctx, int stepper, const FastParams &P, int s
   int rc = SPSS_OK;
   if (f->kind == KIND_CELLS)
   {
+    f->chain = true;  // binning, re-sort, layout, step and control as one dependent chain
     rc = launch_rebuild(ctx, P);
     g.per_rebuild = 0;
   }
   if (rc == SPSS_OK) rc = launch_step(ctx, stepper, P, trigger ? g.rebuild_exec : nullptr);
+  f->chain = false;
   if (rc == SPSS_OK && sampling) rc = launch_sampling(ctx, P, 1);
   const cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
   if (rc != SPSS_OK)

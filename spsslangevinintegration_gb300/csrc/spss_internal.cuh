@@ -40,6 +40,38 @@ struct Status
 void record_cuda_error(cudaError_t e, const char *what, const char *file, int line);
 int check_launch(const char *what);
 
+// Programmatic dependent launch along the kernel chain of a cell-list step
+// graph.  Every kernel that may be launched with the programmatic attribute
+// begins with pdl_enter(): it waits until the kernel before it in the stream
+// has completed and its writes are visible (without the attribute the
+// instruction does nothing).  No kernel triggers its dependents early: with
+// the trigger at the start of every CTA the large cell-list steps ran about
+// 2 % slower (N = 4,194,304: 0.6095 -> 0.6204 ms), without it they gained
+// (0.6059 ms; N = 65,536: 0.0475 -> 0.0437 ms).
+__device__ __forceinline__ void pdl_enter()
+{
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+// A kernel launch, with the programmatic-serialization attribute when `chained`
+// (the kernel must begin with pdl_enter()).
+template<typename... Params, typename... Args>
+inline cudaError_t launch_chained(bool chained, void (*kernel)(Params...), dim3 grid, dim3 block, size_t smem,
+                                  cudaStream_t stream, Args... args)
+{
+  cudaLaunchAttribute attr;
+  attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr.val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cfg.attrs = chained ? &attr : nullptr;
+  cfg.numAttrs = chained ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // ------------------------------------------------------------------ Philox
 
 // Philox4x32-10 (Salmon, Moraes, Dror & Shaw, "Parallel random numbers: as
@@ -222,8 +254,9 @@ struct DeviceArray
 struct Scanner
 {
   std::vector<DeviceArray<int>> levels;
-  int run(const int *in, int *out, int n, cudaStream_t stream, unsigned long long &launches);
-  int run_level(const int *in, int *out, int n, size_t level, cudaStream_t stream, unsigned long long &launches);
+  int run(const int *in, int *out, int n, cudaStream_t stream, unsigned long long &launches, bool chained = false);
+  int run_level(const int *in, int *out, int n, size_t level, cudaStream_t stream, unsigned long long &launches,
+                bool chained);
   void release()
   {
     for (auto &l : levels) l.release();
@@ -239,7 +272,9 @@ struct Binner
   DeviceArray<int> count, offsets, slot, members;
   Scanner scanner;
   int ncell = 0;
-  int run(const int *cell_of, int n, int ncell, cudaStream_t stream, unsigned long long &launches);
+  // chained: launches after the first with the programmatic attribute
+  int run(const int *cell_of, int n, int ncell, cudaStream_t stream, unsigned long long &launches,
+          bool chained = false);
   void release()
   {
     count.release();
